@@ -1,0 +1,505 @@
+// BFS level kernels.  One template per reference kernel family
+// (bfs/edgelist.cu, rev_edgelist.cu, struct_edgelist.cu,
+// rev_struct_edgelist.cu, vertex_push.cu, vertex_pull.cu,
+// vertex_push_warp.cu, vertex_pull_warp.cu), parameterised on the
+// frontier-count reduction of bfs/bfs.hpp:32-116 and on SIDE (emit the next
+// frontier queue and the frontier statistics, needed when levels of
+// different variants follow each other), plus the GB300 variants
+// frontier-push and frontier-pull.
+//
+// Every variant computes the same level relation (exact BFS depths): a
+// vertex at `depth` gives each unvisited out-neighbour depth + 1, and the
+// frontier counter counts each newly visited vertex exactly once.
+#pragma once
+
+#include <cooperative_groups.h>
+#include "bw_internal.cuh"
+
+namespace bw {
+namespace cg = cooperative_groups;
+
+enum Reduction { RED_NORMAL = 0, RED_BULK = 1, RED_WARP = 2, RED_BLOCK = 3 };
+enum EdgeLayout { FWD_SOA = 0, REV_SOA = 1, FWD_AOS = 2, REV_AOS = 3 };
+
+// Hub handling of frontier-push: vertices above HEAVY_DEGREE edges are cut
+// into HUB_CHUNK-edge chunks that any warp of a second kernel can take.
+constexpr uint32_t HEAVY_DEGREE = 256;
+constexpr uint32_t HUB_CHUNK = 256;
+
+__device__ __forceinline__ int level_depth(const BfsArgs &a)
+{ return a.depth >= 0 ? a.depth : *((volatile int32_t *) &a.ctl->depth); }
+
+__device__ __forceinline__ void reset_slot(LevelSlot *s)
+{
+    s->frontier = 0; s->qlen = 0; s->fedges = 0; s->lsum = 0.f; s->lsq = 0.f;
+    s->lmax_bits = 0; s->heavy = 0;
+}
+
+// Frontier counter with the four reference strategies
+// (bfs/bfs.hpp:32-116).  finish() must be reached by every thread.
+template<int RED>
+struct Counter {
+    uint32_t c = 0;
+    __device__ __forceinline__ void hit(uint32_t *g)
+    {
+        if constexpr (RED == RED_NORMAL) atomicAdd(g, 1u);
+        else c++;
+    }
+    __device__ __forceinline__ void finish(uint32_t *g)
+    {
+        if constexpr (RED == RED_BULK) {
+            if (c) atomicAdd(g, c);
+        } else if constexpr (RED == RED_WARP) {
+            uint32_t s = __reduce_add_sync(FULL_MASK, c);
+            if ((threadIdx.x & 31) == 0 && s) atomicAdd(g, s);
+        } else if constexpr (RED == RED_BLOCK) {
+            __shared__ uint32_t part[32];
+            const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            uint32_t s = __reduce_add_sync(FULL_MASK, c);
+            if (lane == 0) part[wid] = s;
+            __syncthreads();
+            if (wid == 0) {
+                s = lane < (blockDim.x >> 5) ? part[lane] : 0u;
+                s = __reduce_add_sync(FULL_MASK, s);
+                if (lane == 0 && s) atomicAdd(g, s);
+            }
+        }
+    }
+};
+
+// Warp-aggregated append of `v` to a queue; safe in divergent code.
+__device__ __forceinline__ void queue_append(uint32_t *q, uint32_t *len, uint32_t v)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(len, g.size());
+    base = g.shfl(base, 0);
+    q[base + g.thread_rank()] = v;
+}
+
+// Side outputs: next frontier queue + frontier degree statistics.
+template<bool SIDE>
+struct Side {
+    unsigned long long fe = 0;
+    float ls = 0.f, lq = 0.f, lm = 0.f;
+    __device__ __forceinline__ void visit(const BfsArgs &a, uint32_t *qnext, LevelSlot *s, uint32_t v)
+    {
+        if constexpr (SIDE) {
+            if (qnext) queue_append(qnext, &s->qlen, v);   // null: statistics only
+            const uint32_t d = a.outdeg[v];
+            const float l = __log2f(1.0f + static_cast<float>(d));
+            fe += d; ls += l; lq += l * l; lm = fmaxf(lm, l);
+        }
+    }
+    __device__ __forceinline__ void finish(LevelSlot *s)
+    {
+        if constexpr (SIDE) {
+            for (int o = 16; o > 0; o >>= 1) {
+                fe += __shfl_xor_sync(FULL_MASK, fe, o);
+                ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+            }
+            if ((threadIdx.x & 31) == 0 && fe) {
+                atomicAdd(&s->fedges, fe);
+                atomicAdd(&s->lsum, ls);
+                atomicAdd(&s->lsq, lq);
+                atomicMax(&s->lmax_bits, __float_as_uint(lm));
+            }
+        }
+    }
+};
+
+// Relax v to nd; true for exactly one caller per newly visited vertex.
+// The plain pre-check only filters: a stale read can only be INF or nd.
+__device__ __forceinline__ bool relax(int32_t *levels, uint32_t v, int32_t nd)
+{
+    return levels[v] > nd && atomicMin(&levels[v], nd) > nd;
+}
+
+__device__ __forceinline__ uint64_t gtid()
+{ return blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; }
+__device__ __forceinline__ uint64_t gthreads()
+{ return uint64_t(gridDim.x) * blockDim.x; }
+
+// ---------------------------------------------------------------------------
+// Edge-list families (bfs/edgelist.cu:3-22, rev_edgelist.cu:3-21,
+// struct_edgelist.cu:3-22, rev_struct_edgelist.cu:3-22).  Every level
+// streams all M edges; edges are read 4 per thread with 16-byte streaming
+// loads (evict-first, so the depth array keeps L2).  The reverse families
+// test the sequential destination first, which skips the random source
+// gather for already-visited destinations.
+// ---------------------------------------------------------------------------
+template<int RED, bool SIDE, int LAYOUT>
+__global__ void __launch_bounds__(512) k_bfs_edge(BfsArgs a)
+{
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    int32_t *lv = a.levels;
+    Counter<RED> cnt;
+    Side<SIDE> side;
+
+    auto edge = [&](uint32_t row, uint32_t col) {
+        // FWD: row = source, col = destination.  REV: row = destination,
+        // col = source.
+        if constexpr (LAYOUT == FWD_SOA || LAYOUT == FWD_AOS) {
+            if (lv[row] == depth && relax(lv, col, nd)) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, col); }
+        } else {
+            if (lv[row] > nd && lv[col] == depth && atomicMin(&lv[row], nd) > nd) {
+                cnt.hit(&slot->frontier);
+                side.visit(a, qnext, slot, row);
+            }
+        }
+    };
+
+    const uint64_t m = a.m;
+    bool aligned;
+    if constexpr (LAYOUT == FWD_SOA) aligned = !((reinterpret_cast<uintptr_t>(a.fwd_in) | reinterpret_cast<uintptr_t>(a.fwd_e)) & 15);
+    else if constexpr (LAYOUT == REV_SOA) aligned = !((reinterpret_cast<uintptr_t>(a.rev_in) | reinterpret_cast<uintptr_t>(a.rev_e)) & 15);
+    else if constexpr (LAYOUT == FWD_AOS) aligned = !(reinterpret_cast<uintptr_t>(a.fwd_s) & 15);
+    else aligned = !(reinterpret_cast<uintptr_t>(a.rev_s) & 15);
+    const uint64_t groups = aligned ? m >> 2 : 0;
+    const uint64_t stride = gthreads();
+    for (uint64_t g = gtid(); g < groups; g += stride) {
+        if constexpr (LAYOUT == FWD_SOA || LAYOUT == REV_SOA) {
+            const uint32_t *rows = LAYOUT == FWD_SOA ? a.fwd_in : a.rev_in;
+            const uint32_t *cols = LAYOUT == FWD_SOA ? a.fwd_e : a.rev_e;
+            const uint4 r = __ldcs(reinterpret_cast<const uint4 *>(rows) + g);
+            const uint4 c = __ldcs(reinterpret_cast<const uint4 *>(cols) + g);
+            edge(r.x, c.x); edge(r.y, c.y); edge(r.z, c.z); edge(r.w, c.w);
+        } else {
+            const uint2 *pairs = LAYOUT == FWD_AOS ? a.fwd_s : a.rev_s;
+            const uint4 p0 = __ldcs(reinterpret_cast<const uint4 *>(pairs) + 2 * g);
+            const uint4 p1 = __ldcs(reinterpret_cast<const uint4 *>(pairs) + 2 * g + 1);
+            edge(p0.x, p0.y); edge(p0.z, p0.w); edge(p1.x, p1.y); edge(p1.z, p1.w);
+        }
+    }
+    for (uint64_t e = (groups << 2) + gtid(); e < m; e += stride) {
+        if constexpr (LAYOUT == FWD_SOA) edge(a.fwd_in[e], a.fwd_e[e]);
+        else if constexpr (LAYOUT == REV_SOA) edge(a.rev_in[e], a.rev_e[e]);
+        else if constexpr (LAYOUT == FWD_AOS) edge(a.fwd_s[e].x, a.fwd_s[e].y);
+        else edge(a.rev_s[e].x, a.rev_s[e].y);
+    }
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// vertex-push (bfs/vertex_push.cu:3-26): thread per vertex; a frontier
+// vertex's owner walks its CSR row.  Depths are scanned 4 per thread.
+// ---------------------------------------------------------------------------
+template<int RED, bool SIDE>
+__global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
+{
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    int32_t *lv = a.levels;
+    Counter<RED> cnt;
+    Side<SIDE> side;
+    const uint64_t n = a.n, stride = gthreads();
+    auto expand = [&](uint64_t v) {
+        const uint32_t s = a.fwd_v[v], e = a.fwd_v[v + 1];
+        for (uint32_t i = s; i < e; i++) {
+            const uint32_t u = __ldg(a.fwd_e + i);
+            if (relax(lv, u, nd)) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, u); }
+        }
+    };
+    const uint64_t groups = (reinterpret_cast<uintptr_t>(lv) & 15) ? 0 : n >> 2;
+    for (uint64_t g = gtid(); g < groups; g += stride) {
+        const int4 l = reinterpret_cast<const int4 *>(lv)[g];
+        if (l.x == depth) expand(4 * g);
+        if (l.y == depth) expand(4 * g + 1);
+        if (l.z == depth) expand(4 * g + 2);
+        if (l.w == depth) expand(4 * g + 3);
+    }
+    for (uint64_t v = (groups << 2) + gtid(); v < n; v += stride)
+        if (lv[v] == depth) expand(v);
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// vertex-pull (bfs/vertex_pull.cu:3-31): thread per vertex; an unvisited
+// vertex scans its reverse row and stops at the first parent at `depth`.
+// ---------------------------------------------------------------------------
+template<int RED, bool SIDE>
+__global__ void __launch_bounds__(512) k_bfs_vertex_pull(BfsArgs a)
+{
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    int32_t *lv = a.levels;
+    Counter<RED> cnt;
+    Side<SIDE> side;
+    const uint64_t n = a.n, stride = gthreads();
+    auto pull = [&](uint64_t v) {
+        const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
+        for (uint32_t i = s; i < e; i++) {
+            if (lv[__ldg(a.rev_e + i)] == depth) {
+                lv[v] = nd;
+                cnt.hit(&slot->frontier);
+                side.visit(a, qnext, slot, static_cast<uint32_t>(v));
+                break;
+            }
+        }
+    };
+    const uint64_t groups = (reinterpret_cast<uintptr_t>(lv) & 15) ? 0 : n >> 2;
+    for (uint64_t g = gtid(); g < groups; g += stride) {
+        const int4 l = reinterpret_cast<const int4 *>(lv)[g];
+        if (l.x > nd) pull(4 * g);
+        if (l.y > nd) pull(4 * g + 1);
+        if (l.z > nd) pull(4 * g + 2);
+        if (l.w > nd) pull(4 * g + 3);
+    }
+    for (uint64_t v = (groups << 2) + gtid(); v < n; v += stride)
+        if (lv[v] > nd) pull(v);
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// Virtual-warp families (bfs/vertex_push_warp.cu:19-60,
+// vertex_pull_warp.cu:17-71): a virtual warp of W lanes (W | 32) takes a
+// chunk of C vertices, stages their depths and row offsets in shared memory
+// ((W-lane group) x (C + C + 1) words, ImplementationTemplate.hpp:166-167)
+// and expands / scans each row with its W lanes.  The pull form stops a
+// row as soon as any lane has found a parent (the reference scans the
+// whole row) and writes back only the depths it changed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned subwarp_mask(uint32_t W)
+{
+    if (W >= 32) return FULL_MASK;
+    const unsigned lane = threadIdx.x & 31;
+    return ((1u << W) - 1u) << (lane & ~(W - 1u));
+}
+
+template<int RED, bool SIDE, bool PULL>
+__global__ void __launch_bounds__(512) k_bfs_vwarp(BfsArgs a)
+{
+    extern __shared__ uint32_t smem[];
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    int32_t *lv = a.levels;
+    Counter<RED> cnt;
+    Side<SIDE> side;
+
+    const uint32_t W = a.warp_size, C = a.chunk_size;
+    const uint32_t per_block = blockDim.x / W;
+    const uint32_t vw = threadIdx.x / W, lane = threadIdx.x % W;
+    const unsigned mask = subwarp_mask(W);
+    int32_t *my_lv = reinterpret_cast<int32_t *>(smem) + vw * C;
+    uint32_t *my_off = smem + per_block * C + vw * (C + 1);
+    const uint32_t *V = PULL ? a.rev_v : a.fwd_v;
+    const uint32_t *E = PULL ? a.rev_e : a.fwd_e;
+    const uint64_t n = a.n;
+    const uint64_t total_vw = uint64_t(gridDim.x) * per_block;
+
+    for (uint64_t chunk = blockIdx.x * uint64_t(per_block) + vw; chunk * C < n; chunk += total_vw) {
+        const uint64_t v0 = chunk * C;
+        const uint32_t cntv = static_cast<uint32_t>(min(uint64_t(C), n - v0));
+        for (uint32_t i = lane; i < cntv; i += W) my_lv[i] = lv[v0 + i];
+        for (uint32_t i = lane; i < cntv + 1; i += W) my_off[i] = V[v0 + i];
+        __syncwarp(mask);
+        for (uint32_t v = 0; v < cntv; v++) {
+            const uint32_t s = my_off[v], e = my_off[v + 1];
+            if constexpr (!PULL) {
+                if (my_lv[v] == depth) {
+                    for (uint32_t i = s + lane; i < e; i += W) {
+                        const uint32_t u = __ldg(E + i);
+                        if (relax(lv, u, nd)) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, u); }
+                    }
+                }
+            } else {
+                if (my_lv[v] > depth) {
+                    bool found = false;
+                    for (uint32_t base = s; base < e; base += W) {
+                        const uint32_t i = base + lane;
+                        const bool hit = i < e && lv[__ldg(E + i)] == depth;
+                        if (__any_sync(mask, hit)) { found = true; break; }
+                    }
+                    if (found && lane == 0) my_lv[v] = nd;
+                }
+            }
+        }
+        __syncwarp(mask);
+        if constexpr (PULL) {
+            for (uint32_t i = lane; i < cntv; i += W) {
+                if (my_lv[i] == nd && lv[v0 + i] != nd) {
+                    lv[v0 + i] = nd;
+                    cnt.hit(&slot->frontier);
+                    side.visit(a, qnext, slot, static_cast<uint32_t>(v0 + i));
+                }
+            }
+            __syncwarp(mask);
+        }
+    }
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// frontier-push (GB300 variant): top-down over the frontier queue only.
+// A warp takes 32 queue entries; their rows are concatenated (warp prefix
+// sum of degrees) and the warp's lanes sweep the concatenation, so every
+// lane does the same amount of edge work and reads within a row coalesce.
+// Rows above HEAVY_DEGREE are cut into HUB_CHUNK chunks queued for
+// k_bfs_hub_chunks, which spreads a hub over the whole GPU.
+// Always emits the next queue.
+// ---------------------------------------------------------------------------
+template<bool SIDE>
+__global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
+{
+    __shared__ uint32_t s_excl[8][32];
+    __shared__ uint32_t s_start[8][32];
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    const uint32_t *qin = (depth & 1) ? a.q1 : a.q0;
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    const uint32_t qlen = *((volatile uint32_t *) &a.ctl->slot[(depth + 2) % 3].qlen);
+    int32_t *lv = a.levels;
+    Counter<RED_WARP> cnt;
+    Side<SIDE> side;
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+
+    for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
+        const uint64_t i = t + lane;
+        uint32_t v = 0, s = 0, d = 0;
+        if (i < qlen) {
+            v = qin[i];
+            s = a.fwd_v[v];
+            d = a.fwd_v[v + 1] - s;
+        }
+        if (d > HEAVY_DEGREE) {
+            const uint32_t chunks = (d + HUB_CHUNK - 1) / HUB_CHUNK;
+            const uint32_t base = atomicAdd(&slot->heavy, chunks);
+            for (uint32_t c = 0; c < chunks; c++) a.heavy[base + c] = make_uint2(v, s + c * HUB_CHUNK);
+            d = 0;
+        }
+        uint32_t incl = d;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
+            if (lane >= static_cast<unsigned>(o)) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+        s_excl[wib][lane] = incl - d;
+        s_start[wib][lane] = s;
+        __syncwarp();
+        for (uint32_t k = lane; k < total; k += 32) {
+            // owner = last lane with excl <= k
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
+            }
+            const uint32_t u = __ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo]));
+            if (relax(lv, u, nd)) {
+                cnt.hit(&slot->frontier);
+                queue_append(qnext, &slot->qlen, u);
+                if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
+            }
+        }
+        __syncwarp();
+    }
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+template<bool SIDE>
+__global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
+{
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    const uint32_t chunks = *((volatile uint32_t *) &slot->heavy);
+    int32_t *lv = a.levels;
+    Counter<RED_WARP> cnt;
+    Side<SIDE> side;
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    for (uint64_t c = warp; c < chunks; c += warps) {
+        const uint2 h = a.heavy[c];
+        const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
+        for (uint32_t i = h.y + lane; i < end; i += 32) {
+            const uint32_t u = __ldcs(a.fwd_e + i);
+            if (relax(lv, u, nd)) {
+                cnt.hit(&slot->frontier);
+                queue_append(qnext, &slot->qlen, u);
+                if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
+            }
+        }
+    }
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// frontier-pull (GB300 variant): bottom-up.  Each lane owns one unvisited
+// vertex and checks up to 8 in-neighbours on its own; vertices still
+// unresolved with longer rows are then swept by the whole warp 32
+// in-neighbours at a time with a ballot early exit, so skewed in-degrees
+// do not serialise a lane.  Emits the next queue when SIDE.
+// ---------------------------------------------------------------------------
+template<bool SIDE>
+__global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
+{
+    const int32_t depth = level_depth(a), nd = depth + 1;
+    LevelSlot *slot = &a.ctl->slot[depth % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
+    uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
+    int32_t *lv = a.levels;
+    Counter<RED_WARP> cnt;
+    Side<SIDE> side;
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    const uint64_t n = a.n;
+    constexpr uint32_t SOLO = 8;
+
+    for (uint64_t t = warp * 32; t < n; t += warps * 32) {
+        const uint64_t v = t + lane;
+        bool open = v < n && lv[v] > nd;
+        bool found = false;
+        uint32_t s = 0, e = 0;
+        if (open) {
+            s = a.rev_v[v];
+            e = a.rev_v[v + 1];
+            const uint32_t lim = min(e, s + SOLO);
+            for (uint32_t i = s; i < lim; i++) {
+                if (lv[__ldg(a.rev_e + i)] == depth) { found = true; break; }
+            }
+            open = !found && e > lim;
+            s = lim;
+        }
+        unsigned pending = __ballot_sync(FULL_MASK, open);
+        while (pending) {
+            const int owner = __ffs(pending) - 1;
+            pending &= pending - 1;
+            const uint32_t rs = __shfl_sync(FULL_MASK, s, owner);
+            const uint32_t re = __shfl_sync(FULL_MASK, e, owner);
+            bool got = false;
+            for (uint32_t b = rs; b < re; b += 32) {
+                const uint32_t i = b + lane;
+                const bool hit = i < re && lv[__ldg(a.rev_e + i)] == depth;
+                if (__any_sync(FULL_MASK, hit)) { got = true; break; }
+            }
+            if (lane == static_cast<unsigned>(owner)) found = got;
+        }
+        if (found) {
+            lv[v] = nd;
+            cnt.hit(&slot->frontier);
+            side.visit(a, qnext, slot, static_cast<uint32_t>(v));
+        }
+    }
+    cnt.finish(&slot->frontier);
+    side.finish(slot);
+}
+
+}  // namespace bw

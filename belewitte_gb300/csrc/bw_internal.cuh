@@ -1,0 +1,151 @@
+// Internal declarations shared by the CUDA translation units of
+// libbelewitte_gb300.so.  Not part of the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <climits>
+#include <cuda_runtime.h>
+
+#include "belewitte_gb300.h"
+
+namespace bw {
+
+constexpr int32_t INF = INT32_MAX;
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Error handling: every CUDA call is checked, the message is kept per thread
+// and the C ABI returns BW_ERR_CUDA (the reference prints and exits instead,
+// CUDA.cpp:7-26).
+// ---------------------------------------------------------------------------
+void set_last_error(cudaError_t e, const char *what);
+
+#define BW_CUDA(call)                                                       \
+    do {                                                                    \
+        cudaError_t bw_err_ = (call);                                       \
+        if (bw_err_ != cudaSuccess) {                                       \
+            ::bw::set_last_error(bw_err_, #call);                           \
+            return bw_err_ == cudaErrorMemoryAllocation                     \
+                       ? BW_ERR_OUT_OF_MEMORY : BW_ERR_CUDA;                \
+        }                                                                   \
+    } while (0)
+
+#define BW_TRY(expr)                                                        \
+    do {                                                                    \
+        int bw_rc_ = (expr);                                                \
+        if (bw_rc_ != BW_OK) return bw_rc_;                                 \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// BFS device control block.  A level L accumulates into slot[L % 3], reads
+// the length of its input frontier queue from slot[(L + 2) % 3] and block 0
+// zeroes slot[(L + 1) % 3] for the next level, so no separate reset launch
+// (the reference's resetFrontier(), bfs/bfs.cu:7-11) is needed per level.
+// ---------------------------------------------------------------------------
+struct LevelSlot {
+    uint32_t frontier;            // reference `frontier` counter
+    uint32_t qlen;                // next frontier queue length
+    unsigned long long fedges;    // sum of out-degrees of new vertices
+    float lsum;                   // sum log2(1+deg)
+    float lsq;                    // sum log2(1+deg)^2
+    uint32_t lmax_bits;           // max log2(1+deg) as float bits
+    uint32_t heavy;               // hub chunks queued (frontier-push)
+};
+
+struct BfsCtl {
+    LevelSlot slot[3];
+    int32_t depth;                // level being run (device-loop mode)
+    uint32_t levels_done;
+    int32_t variant;              // variant of the next level (device loop)
+    uint32_t status;              // 0 ok, BW_ERR_LEVEL_LIMIT
+    unsigned long long visited;   // running totals (device loop)
+    unsigned long long traversed;
+    uint32_t max_levels;
+    uint32_t pad[3];
+};
+
+struct BfsArgs {
+    const uint32_t *fwd_v, *fwd_e, *rev_v, *rev_e;
+    const uint32_t *fwd_in, *rev_in;
+    const uint2 *fwd_s, *rev_s;
+    const uint32_t *outdeg;       // out-degree per vertex (side statistics)
+    uint64_t n, m;
+    int32_t *levels;
+    BfsCtl *ctl;
+    uint32_t *q0, *q1;            // frontier queues, parity = depth & 1
+    uint2 *heavy;                 // hub chunk queue {vertex, first edge}
+    int32_t depth;                // >= 0: this level; < 0: read ctl->depth
+    uint32_t warp_size, chunk_size;
+};
+
+// ---------------------------------------------------------------------------
+// PageRank scratch
+// ---------------------------------------------------------------------------
+struct PrCtl {
+    float diff;                   // reference `diff` (pagerank/pagerank.cu:4)
+    uint32_t pad[7];
+};
+
+}  // namespace bw
+
+// The opaque context of the C ABI.
+struct bw_context {
+    int device = 0;
+    int sm_count = 0;
+    int max_threads_per_block = 1024;
+    size_t max_smem_per_block = 0;
+    size_t max_smem_optin = 0;
+
+    // BFS scratch
+    bw::BfsCtl *bfs_ctl = nullptr;        // device
+    bw::BfsCtl *bfs_ctl_host = nullptr;   // pinned mirror for read-back
+    uint32_t *queue[2] = {nullptr, nullptr};
+    uint2 *heavy = nullptr;
+    uint64_t bfs_n_cap = 0, heavy_cap = 0;
+    uint32_t *outdeg = nullptr;
+    uint64_t outdeg_cap = 0;
+    const uint32_t *outdeg_key = nullptr; // fwd_vertices the degrees belong to
+    uint64_t outdeg_key_n = 0;
+
+    // PageRank scratch
+    float *pr_acc = nullptr, *pr_buf[2] = {nullptr, nullptr};
+    uint32_t *pr_deg = nullptr;
+    float *pr_diffs = nullptr;            // per-iteration diff (device)
+    uint64_t pr_n_cap = 0;
+    uint32_t pr_diff_cap = 0;
+
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaEvent_t *level_events = nullptr;
+    uint32_t level_event_cap = 0;
+};
+
+namespace bw {
+
+int ensure_bfs_scratch(bw_context *ctx, uint64_t n, uint64_t m);
+int ensure_outdeg(bw_context *ctx, const bw_graph_view *g, cudaStream_t s);
+int ensure_pr_scratch(bw_context *ctx, uint64_t n, uint32_t iterations);
+int ensure_level_events(bw_context *ctx, uint32_t count);
+
+inline cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+// Persistent-style default grid: `per_sm` blocks per SM.
+inline unsigned default_grid(const bw_context *ctx, unsigned per_sm)
+{ return static_cast<unsigned>(ctx->sm_count) * per_sm; }
+
+// deg[v] = off[v+1] - off[v]
+__global__ void k_row_lengths(const uint32_t *__restrict__ off, uint64_t n,
+                              uint32_t *__restrict__ deg);
+
+using BfsKernelFn = void (*)(BfsArgs);
+// Instantiation tables (bfs_edge.cu, bfs_vertex.cu).
+BfsKernelFn bfs_edge_kernel(int layout, int reduction, bool side);
+BfsKernelFn bfs_vertex_kernel(int family, int reduction, bool side);
+BfsKernelFn bfs_frontier_push_kernel(bool side);
+BfsKernelFn bfs_hub_kernel(bool side);
+BfsKernelFn bfs_frontier_pull_kernel(bool side);
+
+// Reference Backend::computeDivision (Backend.cpp:52-70).
+void compute_division(uint64_t count, uint32_t sm, uint32_t max_tpb,
+                      uint32_t *block, uint32_t *grid);
+
+}  // namespace bw

@@ -1,0 +1,367 @@
+/*
+ * belewitte_gb300.h -- C ABI of the GB300 (sm_103a) BFS and PageRank kernel
+ * libraries.
+ *
+ * Everything here is plain C: pointers, sizes and status codes.  Device
+ * pointers are CUDA global-memory addresses owned by the caller; the library
+ * never frees caller memory.  The only memory the library owns is the scratch
+ * of a bw_context (frontier queues, counters, degree and rank buffers, CUDA
+ * graphs), released by bw_context_destroy().  Streams are passed as `void *`
+ * holding a cudaStream_t (NULL = legacy default stream).
+ *
+ * The reference drives its kernels through a C++ plugin surface
+ * (ImplementationTemplate.hpp GraphKernel::operator() -> CUDABackend::runKernel,
+ * CUDA.hpp:256-263) with per-algorithm device globals for the frontier / diff
+ * counters (bfs/bfs.cu:5-18, pagerank/pagerank.cu:4-17).  Each entry point
+ * below names the reference interface it replaces.  Errors are returned as
+ * status codes instead of the reference's print-and-exit (CUDA.cpp:7-26,
+ * utils/Util.hpp:67-74).
+ */
+#ifndef BELEWITTE_GB300_H
+#define BELEWITTE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                              */
+/* ------------------------------------------------------------------------ */
+enum bw_status {
+    BW_OK = 0,
+    BW_ERR_INVALID_ARGUMENT = 1,    /* NULL pointer, size out of range, ... */
+    BW_ERR_MISSING_REPRESENTATION = 2, /* variant needs a rep the view lacks */
+    BW_ERR_UNKNOWN_VARIANT = 3,
+    BW_ERR_CUDA = 4,                /* a CUDA runtime call failed */
+    BW_ERR_OUT_OF_MEMORY = 5,
+    BW_ERR_LEVEL_LIMIT = 6,         /* traversal exceeded its level cap */
+    BW_ERR_TOO_LARGE = 7,           /* counts beyond the uint32 format */
+    BW_ERR_IO = 8,                  /* graph file could not be read/written */
+    BW_ERR_FORMAT = 9,              /* graph file is malformed */
+    BW_ERR_NO_DEVICE = 10
+};
+
+/* Human readable text of a status code (static storage). */
+const char *bw_status_string(int status);
+/* Text of the last CUDA error seen by this thread (static storage). */
+const char *bw_last_error(void);
+/* Library version / commit stamp; reference: Algorithm.hpp:8 KERNEL_COMMIT. */
+const char *bw_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Graph representations                                                     */
+/* ------------------------------------------------------------------------ */
+/*
+ * Device view of one graph in every representation the reference's
+ * GraphLoader builds (GraphLoader.hpp:123-211, GraphRep.hpp:9-73).
+ * All arrays are uint32, in device memory, and any pointer may be NULL when
+ * no selected variant needs it.
+ *
+ *   CSR forward   : fwd_vertices[N+1], fwd_edges[M]   (rows = sources)
+ *   CSR reverse   : rev_vertices[N+1], rev_edges[M]   (rows = destinations,
+ *                   each row sorted by source id)
+ *   EdgeList fwd  : inEdges = fwd_in_edges[M] (source), outEdges = fwd_edges
+ *   EdgeList rev  : inEdges = rev_in_edges[M] (destination),
+ *                   outEdges = rev_edges (source)
+ *   StructEdgeList: {in,out} pairs, fwd_struct_edges[2M] / rev_struct_edges[2M]
+ *
+ * For a symmetric graph the forward and reverse arrays may alias.
+ */
+typedef struct bw_graph_view {
+    uint64_t vertex_count;
+    uint64_t edge_count;
+    const uint32_t *fwd_vertices;
+    const uint32_t *fwd_edges;
+    const uint32_t *rev_vertices;
+    const uint32_t *rev_edges;
+    const uint32_t *fwd_in_edges;
+    const uint32_t *rev_in_edges;
+    const uint32_t *fwd_struct_edges;
+    const uint32_t *rev_struct_edges;
+} bw_graph_view;
+
+/*
+ * Host graph in CSR form (forward + reverse), allocated by the library with
+ * malloc and released by bw_host_graph_free().  Replaces the mmapped
+ * Graph<V,E> of utils/Graph.hpp:977-1063 as the in-memory form.
+ */
+typedef struct bw_host_graph {
+    uint64_t vertex_count;
+    uint64_t edge_count;
+    int32_t undirected;        /* 1: reverse arrays alias the forward ones */
+    int32_t reserved;
+    uint32_t *fwd_vertices;
+    uint32_t *fwd_edges;
+    uint32_t *rev_vertices;
+    uint32_t *rev_edges;
+} bw_host_graph;
+
+void bw_host_graph_free(bw_host_graph *g);
+
+/*
+ * Build a graph from a directed edge list (host arrays).  Self-loops are
+ * dropped when BW_BUILD_DROP_SELF_LOOPS is set, duplicate edges are removed
+ * when BW_BUILD_DEDUPE is set, and every edge (u,v) gains (v,u) when
+ * BW_BUILD_SYMMETRISE is set.  Rows come out sorted by neighbour id, which
+ * is the order utils/Graph.hpp:1146-1151 (output -> sort -> writeEdges)
+ * produces.
+ */
+enum bw_build_flags {
+    BW_BUILD_DROP_SELF_LOOPS = 1,
+    BW_BUILD_DEDUPE = 2,
+    BW_BUILD_SYMMETRISE = 4
+};
+int bw_graph_from_edges(uint64_t vertex_count, uint64_t count,
+                        const uint32_t *src, const uint32_t *dst, int flags,
+                        bw_host_graph *out);
+
+/*
+ * Seeded synthetic generators (counter-based hashing, so the same seed gives
+ * the same graph on every machine and thread count).  All drop self-loops and
+ * duplicate edges.
+ *   R-MAT(a,b,c,d=1-a-b-c), 2^scale vertices, edge_factor*2^scale samples.
+ *   Erdos-Renyi G(n,m): m uniform (u,v) samples.
+ *   2-D 4-neighbour grid h x w, both directions (evolve/gen-graph.cpp:96-123).
+ *   Barabasi-Albert: n vertices, m attachments each, both directions.
+ */
+int bw_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
+                     double c, uint64_t seed, int symmetrise,
+                     bw_host_graph *out);
+int bw_generate_er(uint64_t n, uint64_t m, uint64_t seed, int symmetrise,
+                   bw_host_graph *out);
+int bw_generate_grid(uint32_t h, uint32_t w, bw_host_graph *out);
+int bw_generate_ba(uint64_t n, uint32_t m, uint64_t seed, bw_host_graph *out);
+
+/*
+ * Device-resident graph in forward + reverse CSR, produced by the device
+ * generators below and released with bw_device_graph_free().  The arrays
+ * are device pointers; for an undirected graph the reverse arrays alias
+ * the forward ones.
+ */
+typedef struct bw_device_graph {
+    uint64_t vertex_count;
+    uint64_t edge_count;
+    int32_t undirected;
+    int32_t reserved;
+    uint32_t *fwd_vertices;
+    uint32_t *fwd_edges;
+    uint32_t *rev_vertices;
+    uint32_t *rev_edges;
+} bw_device_graph;
+
+/*
+ * The same seeded generators evaluated on the GPU (identical counter-based
+ * hash, so they return exactly the graph the host generators return).
+ * kind: 0 R-MAT(p0 = scale, p1 = edge factor, a, b, c),
+ *       1 Erdos-Renyi(p0 = n, p1 = m),
+ *       2 grid(p0 = h, p1 = w),
+ *       3 Barabasi-Albert(p0 = n, p1 = m).
+ * Sorting uses CUB radix sort (input preparation, not a hot path).
+ */
+int bw_generate_device(int kind, uint64_t p0, uint64_t p1, double a, double b,
+                       double c, uint64_t seed, int symmetrise,
+                       bw_device_graph *out, void *stream);
+void bw_device_graph_free(bw_device_graph *g);
+
+/*
+ * The reference's .graph file format, versions 0 and 1
+ * (utils/Graph.hpp:784-807 header/size rules, 977-1063 reader,
+ * 1112-1120 writer).  Only 4-byte vertex/edge fields are supported (the
+ * 8-byte form exists only for graphs beyond uint32 counts).
+ */
+int bw_graph_file_read(const char *path, bw_host_graph *out);
+int bw_graph_file_write(const char *path, const bw_host_graph *g);
+
+/*
+ * Degree statistics of graph-details / SwitchImplementation::loadGraph
+ * (graph-details.cpp:36-61, ImplementationTemplate.hpp:622-649,
+ * utils/StatisticalSummary.hpp:8-80).  kind: 0 = abs, 1 = in, 2 = out.
+ * out[7] = {min, lower quantile, mean, median, upper quantile, max, stddev}.
+ */
+int bw_degree_statistics(const bw_host_graph *g, int kind, double out[7]);
+
+/* ------------------------------------------------------------------------ */
+/* Context                                                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct bw_context bw_context;
+
+/* Select `device` and create a context.  Replaces CUDABackend::setDevice
+ * (CUDA.cpp:158-193) plus the per-algorithm device globals. */
+int bw_context_create(int device, bw_context **out);
+int bw_context_destroy(bw_context *ctx);
+/* Device properties the launch geometry uses. */
+int bw_context_sm_count(const bw_context *ctx);
+
+/*
+ * Launch geometry.  Zero fields take defaults.  block/grid = 0 selects the
+ * reference's Backend::computeDivision (Backend.cpp:52-70) for the reference
+ * variants and an SM-multiple persistent grid for the others.  warp_size /
+ * chunk_size are the -w / -c options of the warp variants
+ * (ImplementationTemplate.hpp:431-436, defaults 32/32).
+ */
+typedef struct bw_launch_config {
+    uint32_t block_size;
+    uint32_t grid_size;
+    uint32_t warp_size;
+    uint32_t chunk_size;
+} bw_launch_config;
+
+/* Reference Backend::computeDivision for `count` items. */
+void bw_compute_division(uint64_t count, uint32_t sm_count,
+                         uint32_t max_threads_per_block,
+                         uint32_t *block_out, uint32_t *grid_out);
+
+/* Expand a CSR (device) into the EdgeList inEdges array (row id per edge)
+ * and build the StructEdgeList {in,out} array; GraphLoader.hpp:134-143. */
+int bw_expand_edge_list(const uint32_t *vertices, uint64_t vertex_count,
+                        uint64_t edge_count, uint32_t *in_edges, void *stream);
+int bw_build_struct_edges(const uint32_t *in_edges, const uint32_t *out_edges,
+                          uint64_t edge_count, uint32_t *struct_edges,
+                          void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* BFS                                                                       */
+/* ------------------------------------------------------------------------ */
+/*
+ * Variants.  Ids 0..31 are the reference's 32 names
+ * (bfs/bfs.cpp:121-207): family * 4 + reduction with
+ *   family    0 edge-list, 1 rev-edge-list, 2 struct-edge-list,
+ *             3 rev-struct-edge-list, 4 vertex-push, 5 vertex-pull,
+ *             6 vertex-push-warp, 7 vertex-pull-warp
+ *   reduction 0 "" (per-visit atomic), 1 -bulk, 2 -warpreduce,
+ *             3 -blockreduce                       (bfs/bfs.hpp:32-116)
+ * Ids >= 32 are GB300 variants with no reference counterpart:
+ *   32 frontier-push   (queue-driven top-down, warp/grid cooperative hubs)
+ *   33 frontier-pull   (bottom-up over unvisited vertices, early exit)
+ */
+enum { BW_BFS_REFERENCE_VARIANTS = 32 };
+int bw_bfs_variant_count(void);
+const char *bw_bfs_variant_name(int variant);
+int bw_bfs_variant_lookup(const char *name);     /* -1 when unknown */
+/* Which representation a variant reads: bit0 fwd CSR, bit1 rev CSR,
+ * bit2 fwd EdgeList, bit3 rev EdgeList, bit4 fwd Struct, bit5 rev Struct. */
+int bw_bfs_variant_reps(int variant);
+
+/*
+ * Initialise depths: every vertex INT32_MAX, root 0; resets the frontier
+ * queue to {root}.  Reference: bfs/bfs.cpp:69-76 (host fill + H2D).
+ */
+int bw_bfs_init(bw_context *ctx, uint64_t vertex_count, uint32_t root,
+                int32_t *levels, void *stream);
+
+/*
+ * Run one BFS level at `depth` with `variant`, then read back the number of
+ * vertices it newly visited into *frontier (host).  Replaces
+ * resetFrontier(); kernel(loader, results, curr); getFrontier()
+ * (bfs/bfs.cpp:95-98, bfs/bfs.cu:7-18).
+ */
+int bw_bfs_level(bw_context *ctx, const bw_graph_view *g, int variant,
+                 int32_t *levels, int32_t depth, const bw_launch_config *cfg,
+                 uint32_t *frontier, void *stream);
+
+/* Per-level side statistics the level kernels accumulate (features). */
+typedef struct bw_bfs_level_stats {
+    uint32_t frontier_vertices;   /* newly visited at this level */
+    uint32_t variant;             /* variant that ran the level */
+    uint64_t frontier_edges;      /* sum of out-degrees of those vertices */
+    float log_degree_sum;         /* sum of log2(1+deg) */
+    float log_degree_sq_sum;      /* sum of log2(1+deg)^2 */
+    float log_degree_max;
+    float device_ms;              /* level time, when timing was requested */
+} bw_bfs_level_stats;
+
+typedef struct bw_bfs_result {
+    uint32_t level_count;         /* levels run (last one found nothing) */
+    uint32_t reserved;
+    uint64_t visited;             /* vertices with a finite depth */
+    uint64_t traversed_edges;     /* sum of out-degrees of visited vertices */
+    double device_ms;             /* traversal time on the device */
+} bw_bfs_result;
+
+enum bw_loop_mode {
+    BW_LOOP_HOST = 0,    /* host loop, one frontier read-back per level */
+    BW_LOOP_GRAPH = 1    /* CUDA graph with a device-side conditional loop */
+};
+
+/*
+ * Full traversal from `root` with a fixed variant.  `stats` (optional) gets
+ * one entry per level, up to stats_capacity.  max_levels = 0 means
+ * vertex_count + 1.  Reference: BFS::runImplementation (bfs/bfs.cpp:51-118).
+ */
+int bw_bfs_run(bw_context *ctx, const bw_graph_view *g, int variant,
+               uint32_t root, int32_t *levels, const bw_launch_config *cfg,
+               int loop_mode, uint32_t max_levels, bw_bfs_result *result,
+               bw_bfs_level_stats *stats, uint32_t stats_capacity,
+               void *stream);
+
+/*
+ * Traversal where `schedule[level]` names the variant of each level
+ * (the last entry repeats).  Used to replay predictor choices and the
+ * per-level oracle-best sequence.  Reference analogue: the kernels tuple
+ * swap of SwitchImplementation::predict (ImplementationTemplate.hpp:675-689).
+ */
+int bw_bfs_run_schedule(bw_context *ctx, const bw_graph_view *g,
+                        const int32_t *schedule, uint32_t schedule_len,
+                        uint32_t root, int32_t *levels,
+                        const bw_launch_config *cfg, uint32_t max_levels,
+                        int time_levels, bw_bfs_result *result,
+                        bw_bfs_level_stats *stats, uint32_t stats_capacity,
+                        void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* PageRank                                                                  */
+/* ------------------------------------------------------------------------ */
+/*
+ * Variants 0..9 are the reference's names (pagerank/pagerank.cpp:205-351):
+ *   0 edge-list, 1 rev-edge-list, 2 struct-edge-list, 3 rev-struct-edge-list,
+ *   4 vertex-push, 5 vertex-pull, 6 vertex-push-warp, 7 vertex-pull-warp,
+ *   8 vertex-pull-nodiv, 9 vertex-pull-warp-nodiv
+ * Ids >= 10 are GB300 variants with no reference counterpart:
+ *  10 pull-segmented  (edge-balanced tiles, CTA segmented reduction,
+ *                      consolidation fused; div semantics)
+ */
+enum { BW_PAGERANK_REFERENCE_VARIANTS = 10 };
+int bw_pagerank_variant_count(void);
+const char *bw_pagerank_variant_name(int variant);
+int bw_pagerank_variant_lookup(const char *name);
+int bw_pagerank_variant_reps(int variant);
+
+typedef struct bw_pagerank_result {
+    uint32_t iterations;
+    uint32_t reserved;
+    float last_diff;        /* sum |pr_new - pr_old| of the last iteration */
+    float reserved_f;
+    double device_ms;       /* degrees + all iterations on the device */
+} bw_pagerank_result;
+
+/*
+ * PageRank with damping 0.85 and 1/N initial ranks for exactly `iterations`
+ * iterations (the reference hard-codes 100, pagerank/pagerank.cpp:55).
+ * `ranks` (device, N floats) receives the result.  Degrees are computed
+ * inside the call, as the reference does inside its timed region
+ * (pagerank/pagerank.cpp:102-112).  `diffs` (optional, host) receives the
+ * per-iteration diff the reference reads back (pagerank.cpp:124).
+ */
+int bw_pagerank_run(bw_context *ctx, const bw_graph_view *g, int variant,
+                    uint32_t iterations, float *ranks,
+                    const bw_launch_config *cfg, int loop_mode,
+                    bw_pagerank_result *result, float *diffs, void *stream);
+
+/*
+ * Same, with a per-iteration variant schedule (last entry repeats).  All
+ * scheduled variants must share one semantics class (div or nodiv).
+ */
+int bw_pagerank_run_schedule(bw_context *ctx, const bw_graph_view *g,
+                             const int32_t *schedule, uint32_t schedule_len,
+                             uint32_t iterations, float *ranks,
+                             const bw_launch_config *cfg, int time_iterations,
+                             float *iteration_ms, bw_pagerank_result *result,
+                             void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BELEWITTE_GB300_H */

@@ -1,0 +1,95 @@
+"""PageRank parity on the GPU through the C ABI, every variant.
+
+Tolerances (stated by the requirement this library is built to):
+  * vertex-pull, vertex-pull-nodiv: bit-exact against the oracle (same
+    sequential row order and the same float / double operations);
+  * every other variant: max relative error <= 1e-5 against the oracle of
+    its semantics class (their float atomics / warp reductions reorder the
+    sum), and <= 1e-4 against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import belewitte_gb300 as bw
+import oracle
+from tests.graphs import catalog
+
+pytestmark = pytest.mark.gpu
+
+REL_REF = 1e-5
+REL_F64 = 1e-4
+GRAPHS = ["rmat10", "rmat12_sym", "rmat14", "er", "grid", "ba", "chain", "star", "tiny", "isolated"]
+BITEXACT = {"vertex-pull", "vertex-pull-nodiv"}
+
+
+@pytest.fixture(scope="module")
+def graphs(ctx):
+    out = {}
+    for name in GRAPHS:
+        h = catalog()[name][0]()
+        out[name] = (h, bw.DeviceGraph(h))
+    return out
+
+
+def _oracles(h, it, cache={}):
+    key = (id(h), it)
+    if key not in cache:
+        n = h.vertex_count
+        div, _ = oracle.pagerank(oracle.PR_DIV, n, h.rev_vertices, h.rev_edges, it)
+        nodiv, _ = oracle.pagerank(oracle.PR_NODIV, n, h.rev_vertices, h.rev_edges, it)
+        d64 = oracle.pagerank_f64(oracle.PR_DIV, n, h.rev_vertices, h.rev_edges, it)
+        n64 = oracle.pagerank_f64(oracle.PR_NODIV, n, h.rev_vertices, h.rev_edges, it)
+        cache[key] = (div, nodiv, d64, n64)
+    return cache[key]
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float((np.abs(a - b) / np.abs(b)).max())
+
+
+@pytest.mark.parametrize("variant", list(range(11)))
+@pytest.mark.parametrize("iterations", [1, 30])
+def test_variant_parity(ctx, graphs, variant, iterations):
+    name = bw.pagerank_variant_names()[variant]
+    for gname, (h, g) in graphs.items():
+        run = bw.pagerank(ctx, g, variant, iterations)
+        got = run.ranks.cpu().numpy()
+        div, nodiv, d64, n64 = _oracles(h, iterations)
+        ref, r64 = (nodiv, n64) if "nodiv" in name else (div, d64)
+        if name in BITEXACT:
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (name, gname)
+        else:
+            assert _rel(got, ref) <= REL_REF, (name, gname, _rel(got, ref))
+        assert _rel(got, r64) <= REL_F64, (name, gname)
+
+
+@pytest.mark.parametrize("variant", ["vertex-push-warp", "vertex-pull-warp", "vertex-pull-warp-nodiv"])
+@pytest.mark.parametrize("w,c", [(1, 1), (4, 8), (16, 64), (32, 32)])
+def test_warp_configs(ctx, graphs, variant, w, c):
+    h, g = graphs["rmat14"]
+    run = bw.pagerank(ctx, g, variant, 10, warp=w, chunk=c)
+    div, nodiv, _, _ = _oracles(h, 10)
+    ref = nodiv if "nodiv" in variant else div
+    assert _rel(run.ranks.cpu().numpy(), ref) <= REL_REF
+
+
+def test_switching_schedule(ctx, graphs):
+    """A per-iteration schedule over div variants stays within tolerance."""
+    h, g = graphs["rmat14"]
+    sched = ["edge-list", "vertex-pull", "pull-segmented", "rev-struct-edge-list", "vertex-push-warp",
+             "vertex-pull-warp", "vertex-push", "rev-edge-list", "struct-edge-list"]
+    run = bw.pagerank_schedule(ctx, g, sched, 30, time_iterations=True)
+    div, _, _, _ = _oracles(h, 30)
+    assert _rel(run.ranks.cpu().numpy(), div) <= REL_REF
+    assert len(run.iteration_ms) == 30 and all(t > 0 for t in run.iteration_ms)
+    with pytest.raises(bw.BwError):
+        bw.pagerank_schedule(ctx, g, ["vertex-pull", "vertex-pull-nodiv"], 5)
+
+
+def test_diffs_reported(ctx, graphs):
+    h, g = graphs["rmat10"]
+    run = bw.pagerank(ctx, g, "vertex-pull", 30)
+    _, diffs = oracle.pagerank(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 30)
+    assert np.allclose(run.diffs, diffs, rtol=1e-3, atol=1e-9)
