@@ -91,30 +91,31 @@ def build_core(force: bool = False, jobs: int | None = None) -> Path:
 
 
 def build_plugins(force: bool = False) -> list[Path]:
-    """Build the reference-compatible plugin libraries and kernel-runner."""
+    """Build the reference-compatible plugin libraries and kernel-runner.
+
+    The framework (Algorithm, options, timers) is linked into kernel-runner
+    and exported with -rdynamic; the plugin libraries resolve against it, so
+    the timer registry and the implementation registry are shared.
+    """
     if not PLUGIN.exists():
         return []
-    out = []
-    common = ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", f"-I{PLUGIN}"]
+    cuda_inc = "/usr/local/cuda/include"
+    common = ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", f"-I{PLUGIN}", f"-I{cuda_inc}"]
     rt = [f"-L{PKG}", "-lbelewitte_gb300", f"-Wl,-rpath,{PKG}", "-Wl,-rpath,$ORIGIN",
           "-L/usr/local/cuda/lib64", "-lcudart", "-Wl,-rpath,/usr/local/cuda/lib64", "-ldl"]
-    framework = sorted(str(p) for p in PLUGIN.glob("framework_*.cpp"))
-    headers = list(PLUGIN.glob("*.hpp")) + list(INCLUDE.glob("*.h"))
+    headers = list(PLUGIN.glob("*.hpp")) + list(INCLUDE.glob("*.h")) + [LIB]
     targets = [
         (PKG / "libbfskernel.so", [PLUGIN / "bfs_plugin.cpp"], ["-shared"]),
         (PKG / "libpagerankkernel.so", [PLUGIN / "pagerank_plugin.cpp"], ["-shared"]),
-        (PKG / "kernel-runner", [PLUGIN / "kernel_runner.cpp"], ["-rdynamic"]),
+        (PKG / "kernel-runner", [PLUGIN / "kernel_runner.cpp", PLUGIN / "framework_core.cpp"], ["-rdynamic"]),
     ]
-    steps = []
+    steps, out = [], []
     for target, srcs, extra in targets:
-        if not all(s.exists() for s in srcs):
-            continue
-        deps = srcs + headers + [Path(f) for f in framework]
-        if force or _stale(target, deps):
-            steps.append((target, common + extra + [*map(str, srcs), *framework, "-o", str(target)] + rt))
+        if force or _stale(target, srcs + headers):
+            steps.append(common + extra + [*map(str, srcs), "-o", str(target)] + rt)
         out.append(target)
     with _cf.ThreadPoolExecutor(max_workers=3) as ex:
-        list(ex.map(lambda t: _run(t[1]), steps))
+        list(ex.map(_run, steps))
     return out
 
 

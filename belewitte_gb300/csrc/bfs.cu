@@ -156,7 +156,7 @@ int plan_launch(const bw_context *ctx, int variant, bool side, const bw_launch_c
         if (cfg->block_size % 32 || cfg->block_size > 1024) return BW_ERR_INVALID_ARGUMENT;
         if ((variant == V_FRONTIER_PUSH || variant == V_FRONTIER_PULL) && cfg->block_size != 256)
             return BW_ERR_INVALID_ARGUMENT;
-        if (variant < 16 && cfg->block_size > 512) return BW_ERR_INVALID_ARGUMENT;
+        if (cfg->block_size > 512) return BW_ERR_INVALID_ARGUMENT;   // __launch_bounds__(512)
         l.block = cfg->block_size;
     }
     if (cfg && cfg->grid_size) l.grid = cfg->grid_size;

@@ -225,41 +225,6 @@ __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
 }
 
 // ----------------------------- pull variants ------------------------------
-// vertex-pull / vertex-pull-nodiv (pagerank/vertex_pull.cu:3-31,
-// vertex_pull_nodiv.cu:3-29): thread per vertex, sequential sum over the
-// reverse row in row order -> bit-identical to the reference; the
-// consolidation is fused (each vertex is finished by its owner).
-template<bool NODIV>
-__global__ void __launch_bounds__(256) k_pr_vertex_pull(PrArgs a)
-{
-    float dsum = 0.0f;
-    const uint64_t n = a.n;
-    const float *src = NODIV ? a.pr_in : a.contrib_in;
-    const float base_nd = nodiv_base(n);
-    for (uint64_t b = (gtid() >> 5) * 32; b < n; b += (gthreads() >> 5) * 32) {
-        const uint64_t v = b + (threadIdx.x & 31);
-        if (v < n) {
-            const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
-            float sum = 0.0f;
-            for (uint32_t i = s; i < e; i++) sum = __fadd_rn(sum, __ldg(src + __ldg(a.rev_e + i)));
-            if constexpr (!NODIV) {
-                const float nr = consolidate_div(sum, n);
-                dsum += fabsf(nr - a.pr_out[v]);
-                a.pr_out[v] = nr;
-                const uint32_t d = a.deg[v];
-                a.contrib_out[v] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
-            } else {
-                float nr = __fmaf_rn(DAMPING, sum, base_nd);
-                dsum += fabsf(nr - a.pr_in[v]);
-                const uint32_t d = a.deg[v];
-                if (d != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(d));
-                a.pr_out[v] = nr;
-            }
-        }
-    }
-    add_diff(a.diff, dsum);
-}
-
 // vertex-pull-warp / -nodiv (pagerank/vertex_pull_warp.cu:4-49,
 // vertex_pull_warp_nodiv.cu:4-47): a virtual warp of W lanes per vertex
 // of a C-vertex chunk; lane-strided partial sums are combined with a
@@ -309,21 +274,35 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
     add_diff(a.diff, dsum);
 }
 
-// ---------------------------- pull-segmented ------------------------------
-// GB300 variant (div semantics).  The reverse CSR is cut once per run into
-// work items of at most 32 consecutive rows and SEG_EDGES edges; a row
-// longer than SEG_LONG edges becomes its own pieces of SEG_EDGES edges.
-// A warp sweeps an item's contiguous edge range 32 edges per step
-// (coalesced index loads, L2-resident contribution gathers), reduces runs
-// of equal rows with a segmented shuffle scan into per-row shared
-// accumulators, and consolidates its rows in the same kernel.  Pieces of
-// split rows meet in acc[] and the last piece to arrive consolidates.
-// Work item: {row_begin, row_end | PIECE flag, edge_begin, edge_end}.
+// ------------------------- work-list pull kernels ---------------------------
+// vertex-pull, vertex-pull-nodiv and pull-segmented share one kernel over a
+// work list cut once per run from the reverse CSR: an item is either at
+// most 32 consecutive rows with at most SEG_EDGES edges (rows of at most
+// SEG_LONG edges), or one long row.  Item: {row_begin, row_end | flags,
+// edge_begin, edge_end}.
+//
+// Short rows: the warp loads the item's indices with unrolled coalesced
+// loads, gathers all contributions at once (up to 1024 independent loads
+// in flight per warp) into shared memory, and then each lane adds its own
+// row's values one after the other in row order -- the reference's
+// sequential summation (pagerank/vertex_pull.cu:23-27), so these rows are
+// bit-identical to it.
+// Long rows, EXACT (vertex-pull, vertex-pull-nodiv): one warp streams the
+// row in 1024-edge chunks (parallel gathers into shared memory) and lane 0
+// keeps the single sequential sum -- bit-identical, bounded by the add
+// chain of the longest row.
+// Long rows, split (pull-segmented): 1024-edge pieces summed by any warp
+// (lane partials + shuffle tree), combined in acc[] by float atomics; the
+// last piece to arrive (arrival counter) consolidates the row.
 constexpr uint32_t SEG_EDGES = 1024;
 constexpr uint32_t SEG_LONG = 256;
-constexpr uint32_t PIECE_FLAG = 0x80000000u;
+constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
+constexpr uint32_t LONG_FLAG = 0x40000000u;    // whole long row
+constexpr uint32_t ROW_MASK = 0x3fffffffu;
+constexpr int PULL_WARPS = 8;                  // warps per block
+constexpr int GATHER_UNROLL = 16;
 
-__global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ counts)
+__global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, int split, uint32_t *__restrict__ counts)
 {
     // one thread per 32-row window: number of work items it will emit
     const uint64_t windows = (n + 31) / 32;
@@ -334,7 +313,7 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32
             const uint32_t d = off[r + 1] - off[r];
             if (d > SEG_LONG) {
                 if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
-                items += (d + SEG_EDGES - 1) / SEG_EDGES;
+                items += split ? (d + SEG_EDGES - 1) / SEG_EDGES : 1;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) { items++; acc_rows = 0; acc_edges = 0; }
@@ -345,7 +324,7 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32
     }
 }
 
-__global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n,
+__global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n, int split,
                            const uint32_t *__restrict__ first, uint4 *__restrict__ work,
                            uint32_t *__restrict__ long_count)
 {
@@ -362,17 +341,19 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n,
                     work[out++] = make_uint4(uint32_t(start_row), uint32_t(r), off[start_row], off[r]);
                     acc_rows = 0; acc_edges = 0;
                 }
-                for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
-                    work[out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | PIECE_FLAG, p,
-                                             min(p + SEG_EDGES, off[r + 1]));
-                long_count[r] = 0;
-                start_row = r + 1;
+                if (split) {
+                    for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
+                        work[out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | PIECE_FLAG, p,
+                                                 min(p + SEG_EDGES, off[r + 1]));
+                    long_count[r] = 0;
+                } else {
+                    work[out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | LONG_FLAG, off[r], off[r + 1]);
+                }
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) {
                 work[out++] = make_uint4(uint32_t(start_row), uint32_t(r), off[start_row], off[r]);
                 acc_rows = 0; acc_edges = 0;
-                start_row = r;
             }
             if (acc_rows == 0) start_row = r;
             acc_rows++; acc_edges += d;
@@ -381,74 +362,130 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n,
     }
 }
 
-__global__ void __launch_bounds__(256) k_pr_pull_segmented(PrArgs a)
+// Consolidate vertex v from its in-sum (div: consolidateRank plus the next
+// contribution; nodiv: consolidateRankNoDiv).  Returns |pr_new - pr_old|.
+template<bool NODIV>
+__device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, float sum, float base_nd)
 {
-    __shared__ float s_acc[8][32];
-    __shared__ uint32_t s_end[8][33];
+    if constexpr (!NODIV) {
+        const float nr = consolidate_div(sum, a.n);
+        const float d = fabsf(nr - a.pr_out[v]);
+        a.pr_out[v] = nr;
+        const uint32_t dg = a.deg[v];
+        a.contrib_out[v] = dg ? __fdiv_rn(nr, static_cast<float>(dg)) : 0.0f;
+        return d;
+    } else {
+        float nr = __fmaf_rn(DAMPING, sum, base_nd);
+        const float d = fabsf(nr - a.pr_in[v]);
+        const uint32_t dg = a.deg[v];
+        if (dg != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(dg));
+        a.pr_out[v] = nr;
+        return d;
+    }
+}
+
+// Gather src[rev_e[e0 + k]] for k in [0, len) (len <= SEG_EDGES) into buf.
+__device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, const float *__restrict__ src,
+                                            uint32_t e0, uint32_t len, float *buf, unsigned lane)
+{
+    for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
+        uint32_t idx[GATHER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < GATHER_UNROLL; u++) {
+            const uint32_t k = base + u * 32 + lane;
+            idx[u] = k < len ? __ldcs(rev_e + e0 + k) : 0u;
+        }
+        float v[GATHER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < GATHER_UNROLL; u++) {
+            const uint32_t k = base + u * 32 + lane;
+            v[u] = k < len ? __ldg(src + idx[u]) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < GATHER_UNROLL; u++) {
+            const uint32_t k = base + u * 32 + lane;
+            if (k < len) buf[k] = v[u];
+        }
+    }
+}
+
+template<bool NODIV, bool EXACT_LONG>
+__global__ void __launch_bounds__(PULL_WARPS * 32) k_pr_pull_items(PrArgs a)
+{
+    __shared__ __align__(16) float s_val[PULL_WARPS][SEG_EDGES];
+    __shared__ uint32_t s_end[PULL_WARPS][33];
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
-    const uint64_t n = a.n;
+    const float *src = NODIV ? a.pr_in : a.contrib_in;
+    const float base_nd = nodiv_base(a.n);
+    float *buf = s_val[wib];
     float dsum = 0.0f;
     for (uint64_t it = warp; it < a.work_count; it += warps) {
         const uint4 w = a.work[it];
-        const bool piece = (w.y & PIECE_FLAG) != 0;
-        const uint32_t r0 = w.x, r1 = w.y & ~PIECE_FLAG, e0 = w.z, e1 = w.w;
-        if (piece) {
+        const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
+        if (w.y & PIECE_FLAG) {
             float part = 0.0f;
-            for (uint32_t i = e0 + lane; i < e1; i += 32) part += __ldg(a.contrib_in + __ldcs(a.rev_e + i));
+            for (uint32_t base = e0; base < e1; base += 32 * GATHER_UNROLL) {
+                uint32_t idx[GATHER_UNROLL];
+#pragma unroll
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t i = base + u * 32 + lane;
+                    idx[u] = i < e1 ? __ldcs(a.rev_e + i) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t i = base + u * 32 + lane;
+                    part += i < e1 ? __ldg(src + idx[u]) : 0.0f;
+                }
+            }
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
             if (lane == 0) {
                 atomicAdd(&a.acc[r0], part);
                 __threadfence();
                 const uint32_t pieces = (a.rev_v[r0 + 1] - a.rev_v[r0] + SEG_EDGES - 1) / SEG_EDGES;
-                const uint32_t arrived = atomicAdd(&a.long_count[r0], 1u) + 1;
-                if (arrived == pieces) {
+                if (atomicAdd(&a.long_count[r0], 1u) + 1 == pieces) {
                     __threadfence();
                     const float total = atomicExch(&a.acc[r0], 0.0f);
                     a.long_count[r0] = 0;
-                    const float nr = consolidate_div(total, n);
-                    dsum += fabsf(nr - a.pr_out[r0]);
-                    a.pr_out[r0] = nr;
-                    const uint32_t d = a.deg[r0];
-                    a.contrib_out[r0] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
+                    dsum += finish_vertex<NODIV>(a, r0, total, base_nd);
                 }
             }
             continue;
         }
-        const uint32_t rows = r1 - r0;
-        // row end offsets of the item's rows, relative to e0
-        if (lane < rows) s_end[wib][lane] = a.rev_v[r0 + lane + 1] - e0;
-        s_acc[wib][lane] = 0.0f;
-        __syncwarp();
-        uint32_t row = 0;   // current row of this lane's edge
-        for (uint32_t b = 0; b < e1 - e0; b += 32) {
-            const uint32_t k = b + lane;
-            const bool valid = k < e1 - e0;
-            float val = 0.0f;
-            if (valid) {
-                while (s_end[wib][row] <= k) row++;
-                val = __ldg(a.contrib_in + __ldcs(a.rev_e + e0 + k));
+        if (w.y & LONG_FLAG) {
+            float sum = 0.0f;
+            for (uint32_t base = e0; base < e1; base += SEG_EDGES) {
+                const uint32_t c = min(SEG_EDGES, e1 - base);
+                gather_into(a.rev_e, src, base, c, buf, lane);
+                __syncwarp();
+                if (lane == 0) {
+                    uint32_t i = 0;
+                    for (; i + 4 <= c; i += 4) {
+                        const float4 q = *reinterpret_cast<const float4 *>(buf + i);
+                        sum = __fadd_rn(sum, q.x); sum = __fadd_rn(sum, q.y);
+                        sum = __fadd_rn(sum, q.z); sum = __fadd_rn(sum, q.w);
+                    }
+                    for (; i < c; i++) sum = __fadd_rn(sum, buf[i]);
+                }
+                __syncwarp();
             }
-            const uint32_t key = valid ? row : 0xffffffffu;
-            for (int o = 1; o < 32; o <<= 1) {
-                const float y = __shfl_down_sync(FULL_MASK, val, o);
-                const uint32_t kk = __shfl_down_sync(FULL_MASK, key, o);
-                if (lane + o < 32 && kk == key) val += y;
-            }
-            const uint32_t prev = __shfl_up_sync(FULL_MASK, key, 1);
-            if (valid && (lane == 0 || prev != key)) s_acc[wib][key] += val;
-            __syncwarp();
+            if (lane == 0) dsum += finish_vertex<NODIV>(a, r0, sum, base_nd);
+            continue;
         }
+        // up to 32 short rows
+        const uint32_t rows = r1 - r0, len = e1 - e0;
+        if (lane < rows) s_end[wib][lane] = a.rev_v[r0 + lane + 1] - e0;
+        gather_into(a.rev_e, src, e0, len, buf, lane);
+        __syncwarp();
         if (lane < rows) {
-            const uint32_t v = r0 + lane;
-            const float nr = consolidate_div(s_acc[wib][lane], n);
-            dsum += fabsf(nr - a.pr_out[v]);
-            a.pr_out[v] = nr;
-            const uint32_t d = a.deg[v];
-            a.contrib_out[v] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
+            const uint32_t b = lane ? s_end[wib][lane - 1] : 0u, e = s_end[wib][lane];
+            float sum = 0.0f;
+            for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
+            dsum += finish_vertex<NODIV>(a, r0 + lane, sum, base_nd);
         }
         __syncwarp();
     }
+    (void) EXACT_LONG;
     add_diff(a.diff, dsum);
 }
 
@@ -537,8 +574,16 @@ Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cf
 int validate_cfg(const bw_context *ctx, int variant, const bw_launch_config *cfg)
 {
     if (!cfg) return BW_OK;
-    if (cfg->block_size && (cfg->block_size % 32 || cfg->block_size > 1024)) return BW_ERR_INVALID_ARGUMENT;
-    if (variant == PR_PULL_SEGMENTED && cfg->block_size && cfg->block_size != 256) return BW_ERR_INVALID_ARGUMENT;
+    if (cfg->block_size && (cfg->block_size % 32 || cfg->block_size > 256)) {
+        // every PageRank kernel is built for at most 256 threads, the warp
+        // variants for 512
+        const bool warp = variant == PR_VERTEX_PUSH_WARP || variant == PR_VERTEX_PULL_WARP ||
+                          variant == PR_VERTEX_PULL_WARP_NODIV;
+        if (cfg->block_size % 32 || cfg->block_size > (warp ? 512u : 256u)) return BW_ERR_INVALID_ARGUMENT;
+    }
+    if ((variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV) &&
+        cfg->block_size && cfg->block_size != PULL_WARPS * 32)
+        return BW_ERR_INVALID_ARGUMENT;
     const uint32_t W = cfg->warp_size ? cfg->warp_size : 32;
     const uint32_t C = cfg->chunk_size ? cfg->chunk_size : 32;
     // ImplementationTemplate.hpp:463-471: power-of-two W <= 32, C % W == 0.
@@ -570,7 +615,7 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
     return BW_OK;
 }
 
-int build_segments(bw_context *ctx, const bw_graph_view *g, PrRun &run, cudaStream_t s)
+int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &run, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count;
     const uint64_t windows = (n + 31) / 32;
@@ -580,9 +625,9 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, PrRun &run, cudaStre
     BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.win_counts), (windows + 1) * sizeof(uint32_t), s));
     BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
     BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
-    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, run.win_counts);
+    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts);
     k_exclusive_scan_small<<<1, 1024, 0, s>>>(run.win_counts, windows, run.win_counts + windows);
-    k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, run.win_counts, run.work, run.long_count);
+    k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts, run.work, run.long_count);
     BW_CUDA(cudaGetLastError());
     uint32_t count = 0;
     BW_CUDA(cudaMemcpyAsync(&count, run.win_counts + windows, sizeof count, cudaMemcpyDeviceToHost, s));
@@ -608,11 +653,11 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_REV_STRUCT_EDGE_LIST: k_pr_edge<3><<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_VERTEX_PUSH: k_pr_vertex_push<<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_VERTEX_PUSH_WARP: k_pr_vertex_push_warp<<<geo.grid, geo.block, geo.smem, s>>>(a); break;
-      case PR_VERTEX_PULL: k_pr_vertex_pull<false><<<geo.grid, geo.block, 0, s>>>(a); break;
-      case PR_VERTEX_PULL_NODIV: k_pr_vertex_pull<true><<<geo.grid, geo.block, 0, s>>>(a); break;
+      case PR_VERTEX_PULL: k_pr_pull_items<false, true><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
+      case PR_VERTEX_PULL_NODIV: k_pr_pull_items<true, true><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
       case PR_VERTEX_PULL_WARP: k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
       case PR_VERTEX_PULL_WARP_NODIV: k_pr_vertex_pull_warp<true><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
-      case PR_PULL_SEGMENTED: k_pr_pull_segmented<<<geo.grid, 256, 0, s>>>(a); break;
+      case PR_PULL_SEGMENTED: k_pr_pull_items<false, false><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
       default: return BW_ERR_UNKNOWN_VARIANT;
     }
     if (!is_fused(variant)) {
@@ -634,14 +679,15 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         return BW_ERR_INVALID_ARGUMENT;
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
-    bool need_seg = false, any_rowlen = false, any_deg = false;
+    bool need_split = false, need_exact = false, any_rowlen = false, any_deg = false;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
         if (v < 0 || v >= PR_VARIANT_COUNT) return BW_ERR_UNKNOWN_VARIANT;
         if (is_nodiv(v) != nodiv) return BW_ERR_INVALID_ARGUMENT;
         BW_TRY(validate_cfg(ctx, v, cfg));
         reps |= kPrReps[v];
-        if (v == PR_PULL_SEGMENTED) need_seg = true;
+        if (v == PR_PULL_SEGMENTED) need_split = true;
+        if (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV) need_exact = true;
         if (uses_rowlen(v)) any_rowlen = true; else any_deg = true;
     }
     BW_TRY(check_reps(g, reps));
@@ -651,8 +697,9 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     BW_TRY(ensure_pr_scratch(ctx, n, iterations));
     if (time_iterations) BW_TRY(ensure_level_events(ctx, iterations + 1));
 
-    PrRun run;
-    if (need_seg) BW_TRY(build_segments(ctx, g, run, s));
+    PrRun split_run, exact_run;
+    if (need_split) BW_TRY(build_segments(ctx, g, 1, split_run, s));
+    if (need_exact) BW_TRY(build_segments(ctx, g, 0, exact_run, s));
 
     PrArgs a{};
     a.fwd_v = g->fwd_vertices; a.fwd_e = g->fwd_edges; a.rev_v = g->rev_vertices; a.rev_e = g->rev_edges;
@@ -664,7 +711,6 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.acc = ctx->pr_acc;
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
     a.chunk_size = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
-    a.work = run.work; a.work_count = run.work_count; a.long_count = run.long_count;
 
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
     // Degrees inside the timed region, as pagerank/pagerank.cpp:102-112.
@@ -708,6 +754,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
                 a.contrib_out = contrib[j & 1];
             }
         }
+        const PrRun &items = v == PR_PULL_SEGMENTED ? split_run : exact_run;
+        a.work = items.work;
+        a.work_count = items.work_count;
+        a.long_count = items.long_count;
         Geometry geo = geometry(ctx, v, cfg);
         BW_TRY(launch_iteration(ctx, v, a, geo, s));
         (void) loop_mode;
@@ -721,7 +771,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         BW_CUDA(cudaMemcpyAsync(&diffs_dev_last, ctx->pr_diffs + iterations - 1, sizeof(float),
                                 cudaMemcpyDeviceToHost, s));
     BW_CUDA(cudaStreamSynchronize(s));
-    free_run(run, s);
+    free_run(split_run, s);
+    free_run(exact_run, s);
     if (time_iterations && iteration_ms) {
         for (uint32_t j = 0; j < iterations; j++)
             BW_CUDA(cudaEventElapsedTime(&iteration_ms[j], ctx->level_events[j], ctx->level_events[j + 1]));

@@ -81,7 +81,7 @@ def test_warp_configs(ctx, graphs, fam, w, c):
 
 def test_launch_geometry_overrides(ctx, graphs):
     h, g, r, lv, cnt = graphs["er"]
-    for v, blk, grd in [("edge-list-blockreduce", 64, 3), ("vertex-pull", 1024, 1), ("vertex-push-bulk", 32, 7)]:
+    for v, blk, grd in [("edge-list-blockreduce", 64, 3), ("vertex-pull", 512, 1), ("vertex-push-bulk", 32, 7)]:
         run = bw.bfs(ctx, g, v, r, block=blk, grid=grd)
         assert np.array_equal(run.levels.cpu().numpy(), lv)
 
