@@ -58,6 +58,17 @@ class PagerankResult(C.Structure):
                 ("device_ms", C.c_double)]
 
 
+class MlpTrainConfig(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("weight_decay", C.c_float), ("reserved", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class SwitchConfig(C.Structure):
+    _fields_ = [("params", C.c_void_p), ("classes", C.c_uint32), ("fallback", C.c_int32),
+                ("candidates", C.POINTER(C.c_int32)), ("threshold", C.c_float), ("reserved", C.c_uint32)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/belewitte_gb300.h
 SIGNATURES = {
     "bw_status_string": (C.c_char_p, [C.c_int]),
@@ -106,6 +117,23 @@ SIGNATURES = {
     "bw_pagerank_run_schedule": (C.c_int, [C.c_void_p, C.POINTER(GraphView), i32p, C.c_uint32,
                                            C.c_uint32, C.c_void_p, C.POINTER(LaunchConfig), C.c_int,
                                            C.POINTER(C.c_float), C.POINTER(PagerankResult), C.c_void_p]),
+    "bw_mlp_param_count": (C.c_uint32, [C.c_uint32]),
+    "bw_bfs_features": (None, [C.c_uint64, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_uint64, C.c_uint64,
+                               C.c_uint64, C.c_uint64, C.c_uint32, C.POINTER(C.c_float)]),
+    "bw_bfs_profile": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_uint32, C.c_void_p, i32p, C.c_uint32,
+                                 C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float),
+                                 C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
+    "bw_mlp_init": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint64,
+                              C.c_void_p]),
+    "bw_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                               C.POINTER(MlpTrainConfig), C.POINTER(C.c_float), C.c_uint32, C.c_void_p]),
+    "bw_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_uint32, C.c_void_p, C.POINTER(C.c_float), C.c_void_p]),
+    "bw_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                 C.c_void_p]),
+    "bw_bfs_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
+                                     C.c_void_p, C.c_int, C.c_uint32, C.POINTER(BfsResult),
+                                     C.POINTER(BfsLevelStats), C.c_uint32, C.c_void_p]),
 }
 
 _lib = None

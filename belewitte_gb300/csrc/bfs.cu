@@ -63,8 +63,12 @@ int check_reps(const bw_graph_view *g, int reps)
     return BW_OK;
 }
 
-__global__ void k_bfs_init(int32_t *levels, uint64_t n, uint32_t root, uint32_t *q0, BfsCtl *ctl,
-                           uint32_t max_levels)
+}  // namespace
+
+// Depth initialisation (bfs/bfs.cpp:69-76) plus the control block; with
+// `outdeg` the root's degree statistics seed the frontier features.
+__global__ void k_bfs_init_side(int32_t *levels, uint64_t n, uint32_t root, uint32_t *q0, BfsCtl *ctl,
+                                uint32_t max_levels, const uint32_t *outdeg)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; v < n; v += stride)
@@ -81,8 +85,19 @@ __global__ void k_bfs_init(int32_t *levels, uint64_t n, uint32_t root, uint32_t 
         ctl->visited = 1;
         ctl->traversed = 0;
         ctl->max_levels = max_levels;
+        if (outdeg) {
+            const uint32_t d = outdeg[root];
+            const float l = __log2f(1.0f + static_cast<float>(d));
+            ctl->slot[2].fedges = d;
+            ctl->slot[2].lsum = l;
+            ctl->slot[2].lsq = l * l;
+            ctl->slot[2].lmax_bits = __float_as_uint(l);
+            ctl->traversed = d;
+        }
     }
 }
+
+namespace {
 
 // Device-loop step: runs after every level inside the conditional body.
 // Logs the level, advances the depth and ends the loop when the level
@@ -256,7 +271,8 @@ int run_host(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule, u
         }
     }
     if (time_levels) BW_TRY(ensure_level_events(ctx, 2));
-    k_bfs_init<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels);
+    k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels,
+                                                     side ? ctx->outdeg : nullptr);
     BW_CUDA(cudaGetLastError());
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
     float total_ms = 0.0f;
@@ -361,7 +377,8 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
         return rc;
     }
 
-    k_bfs_init<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels);
+    k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels,
+                                                     side ? ctx->outdeg : nullptr);
     BW_CUDA(cudaGetLastError());
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
     BW_CUDA(cudaGraphLaunch(exec, s));
@@ -403,6 +420,30 @@ int prepare(bw_context *ctx, const bw_graph_view *g, int reps, bool side, int32_
 }
 
 }  // namespace
+
+// Shared with bw_learn.cu.
+int bfs_prepare(bw_context *ctx, const bw_graph_view *g, int reps, bool side, int32_t *levels, uint32_t root,
+                cudaStream_t s)
+{ return prepare(ctx, g, reps, side, levels, root, s); }
+
+int bfs_plan(const bw_context *ctx, int variant, bool side, const bw_launch_config *cfg, BfsKernelFn *k,
+             BfsKernelFn *k2, unsigned *block, unsigned *grid, size_t *smem)
+{
+    Launch l;
+    BW_TRY(plan_launch(ctx, variant, side, cfg, &l));
+    *k = l.k; *k2 = l.k2; *block = l.block; *grid = l.grid; *smem = l.smem;
+    return BW_OK;
+}
+
+BfsArgs bfs_args(bw_context *ctx, const bw_graph_view *g, int32_t *levels, int32_t depth,
+                 const bw_launch_config *cfg)
+{ return make_args(ctx, g, levels, depth, cfg); }
+
+int bfs_variant_reps(int v) { return variant_reps(v); }
+
+int bfs_traversed(bw_context *ctx, const bw_graph_view *g, int32_t *levels, cudaStream_t s, uint64_t *out)
+{ return traversed_edges(ctx, g, levels, s, out); }
+
 }  // namespace bw
 
 using namespace bw;
@@ -430,8 +471,8 @@ int bw_bfs_init(bw_context *ctx, uint64_t vertex_count, uint32_t root, int32_t *
 {
     if (!ctx || !levels || vertex_count == 0 || root >= vertex_count) return BW_ERR_INVALID_ARGUMENT;
     BW_TRY(ensure_bfs_scratch(ctx, vertex_count, 0));
-    k_bfs_init<<<ctx->sm_count * 4, 256, 0, as_stream(stream)>>>(levels, vertex_count, root, ctx->queue[0],
-                                                                 ctx->bfs_ctl, 0);
+    k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, as_stream(stream)>>>(levels, vertex_count, root, ctx->queue[0],
+                                                                      ctx->bfs_ctl, 0, nullptr);
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }

@@ -71,17 +71,20 @@ struct PrArgs {
     const uint4 *work;         // pull-segmented work items
     uint32_t work_count;
     uint32_t *long_count;      // arrival counters of split rows
+    double base_div;           // (1.0 - 0.85f) / N, computed once on the host
 };
 
 __device__ __forceinline__ uint64_t gtid() { return blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; }
 __device__ __forceinline__ uint64_t gthreads() { return uint64_t(gridDim.x) * blockDim.x; }
 
-__device__ __forceinline__ float consolidate_div(float acc, uint64_t n)
+// pagerank/pagerank.cu:132: new_rank = (float)(((1.0 - d) / N) + (double)(d * acc))
+// -- a double base term (computed once: IEEE division is correctly rounded,
+// so the host value is the one the reference computes per vertex), a float
+// product, one double addition and the rounding to float.
+__device__ __forceinline__ float consolidate_div(float acc, double base)
 {
-    // pagerank/pagerank.cu:132: double base term, float product.
     const float scaled = __fmul_rn(DAMPING, acc);
-    return static_cast<float>((1.0 - static_cast<double>(DAMPING)) / static_cast<double>(n) +
-                              static_cast<double>(scaled));
+    return __double2float_rn(__dadd_rn(base, static_cast<double>(scaled)));
 }
 
 __device__ __forceinline__ float nodiv_base(uint64_t n)
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(256) k_consolidate_div(PrArgs a, int rowlen)
     for (uint64_t base = (gtid() >> 5) * 32; base < n; base += (gthreads() >> 5) * 32) {
         const uint64_t v = base + (threadIdx.x & 31);
         if (v < n) {
-            const float nr = consolidate_div(a.acc[v], n);
+            const float nr = consolidate_div(a.acc[v], a.base_div);
             dsum += fabsf(nr - a.pr_out[v]);
             a.pr_out[v] = nr;
             a.acc[v] = 0.0f;
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
             if (lane == 0) {
                 const uint64_t x = v0 + v;
                 if constexpr (!NODIV) {
-                    const float nr = consolidate_div(part, n);
+                    const float nr = consolidate_div(part, a.base_div);
                     dsum += fabsf(nr - a.pr_out[x]);
                     a.pr_out[x] = nr;
                     const uint32_t d = a.deg[x];
@@ -294,13 +297,13 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
 // Long rows, split (pull-segmented): 1024-edge pieces summed by any warp
 // (lane partials + shuffle tree), combined in acc[] by float atomics; the
 // last piece to arrive (arrival counter) consolidates the row.
-constexpr uint32_t SEG_EDGES = 1024;
+constexpr uint32_t SEG_EDGES = 512;
 constexpr uint32_t SEG_LONG = 256;
 constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
 constexpr uint32_t LONG_FLAG = 0x40000000u;    // whole long row
 constexpr uint32_t ROW_MASK = 0x3fffffffu;
 constexpr int PULL_WARPS = 8;                  // warps per block
-constexpr int GATHER_UNROLL = 16;
+constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
 __global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, int split, uint32_t *__restrict__ counts)
 {
@@ -368,7 +371,7 @@ template<bool NODIV>
 __device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, float sum, float base_nd)
 {
     if constexpr (!NODIV) {
-        const float nr = consolidate_div(sum, a.n);
+        const float nr = consolidate_div(sum, a.base_div);
         const float d = fabsf(nr - a.pr_out[v]);
         a.pr_out[v] = nr;
         const uint32_t dg = a.deg[v];
@@ -410,7 +413,7 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
 }
 
 template<bool NODIV, bool EXACT_LONG>
-__global__ void __launch_bounds__(PULL_WARPS * 32) k_pr_pull_items(PrArgs a)
+__global__ void __launch_bounds__(PULL_WARPS * 32, 5) k_pr_pull_items(PrArgs a)
 {
     __shared__ __align__(16) float s_val[PULL_WARPS][SEG_EDGES];
     __shared__ uint32_t s_end[PULL_WARPS][33];
@@ -453,19 +456,42 @@ __global__ void __launch_bounds__(PULL_WARPS * 32) k_pr_pull_items(PrArgs a)
             continue;
         }
         if (w.y & LONG_FLAG) {
+            // Lane 0 keeps the sequential sum of chunk c while lanes 1..31
+            // gather chunk c + 1 into the other half of the warp's buffer.
+            float *half[2] = {buf, buf + SEG_EDGES / 2};
+            constexpr uint32_t CH = SEG_EDGES / 2;
+            const uint32_t nch = (e1 - e0 + CH - 1) / CH;
+            auto gather31 = [&](uint32_t c, float *dst) {
+                const uint32_t b0 = e0 + c * CH, cnt = min(CH, e1 - b0);
+                if (lane == 0) return;
+                constexpr int U = (CH + 30) / 31;
+                uint32_t idx[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const uint32_t k = (lane - 1) + 31 * u;
+                    idx[u] = k < cnt ? __ldcs(a.rev_e + b0 + k) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const uint32_t k = (lane - 1) + 31 * u;
+                    if (k < cnt) dst[k] = __ldg(src + idx[u]);
+                }
+            };
+            gather31(0, half[0]);
+            __syncwarp();
             float sum = 0.0f;
-            for (uint32_t base = e0; base < e1; base += SEG_EDGES) {
-                const uint32_t c = min(SEG_EDGES, e1 - base);
-                gather_into(a.rev_e, src, base, c, buf, lane);
-                __syncwarp();
+            for (uint32_t c = 0; c < nch; c++) {
+                if (c + 1 < nch) gather31(c + 1, half[(c + 1) & 1]);
                 if (lane == 0) {
+                    const float *q = half[c & 1];
+                    const uint32_t cnt = min(CH, e1 - (e0 + c * CH));
                     uint32_t i = 0;
-                    for (; i + 4 <= c; i += 4) {
-                        const float4 q = *reinterpret_cast<const float4 *>(buf + i);
-                        sum = __fadd_rn(sum, q.x); sum = __fadd_rn(sum, q.y);
-                        sum = __fadd_rn(sum, q.z); sum = __fadd_rn(sum, q.w);
+                    for (; i + 4 <= cnt; i += 4) {
+                        const float4 v = *reinterpret_cast<const float4 *>(q + i);
+                        sum = __fadd_rn(sum, v.x); sum = __fadd_rn(sum, v.y);
+                        sum = __fadd_rn(sum, v.z); sum = __fadd_rn(sum, v.w);
                     }
-                    for (; i < c; i++) sum = __fadd_rn(sum, buf[i]);
+                    for (; i < cnt; i++) sum = __fadd_rn(sum, q[i]);
                 }
                 __syncwarp();
             }
@@ -561,6 +587,8 @@ struct Geometry { unsigned block, grid; size_t smem; };
 Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cfg)
 {
     Geometry g{256, static_cast<unsigned>(ctx->sm_count) * 8, 0};
+    if (variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV || variant == PR_PULL_SEGMENTED)
+        g.grid = static_cast<unsigned>(ctx->sm_count) * 5;   // one resident wave (register bound)
     const uint32_t W = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
     const uint32_t C = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
     if (cfg && cfg->block_size) g.block = cfg->block_size;
@@ -707,6 +735,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.fwd_s = reinterpret_cast<const uint2 *>(g->fwd_struct_edges);
     a.rev_s = reinterpret_cast<const uint2 *>(g->rev_struct_edges);
     a.n = n; a.m = g->edge_count;
+    a.base_div = (1.0 - static_cast<double>(0.85f)) / static_cast<double>(n);
     a.deg = ctx->pr_deg;
     a.acc = ctx->pr_acc;
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;

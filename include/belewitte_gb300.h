@@ -361,6 +361,106 @@ int bw_pagerank_run_schedule(bw_context *ctx, const bw_graph_view *g,
                              float *iteration_ms, bw_pagerank_result *result,
                              void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Learned variant switching                                                 */
+/* ------------------------------------------------------------------------ */
+/*
+ * A small MLP (12 -> 64 -> 64 -> K, ReLU, softmax, FP32) picks the variant
+ * of each BFS level from 12 per-level features.  It has no counterpart in
+ * the reference's kernels; it plays the role of the reference's predictor
+ * .so (ImplementationTemplate.hpp:768-827, lookup()), evaluated on the
+ * device.  Parameters live in one device float array:
+ *   mu[12], sd[12] (feature normalisation), W1[64][12], b1[64],
+ *   W2[64][64], b2[64], W3[K][64], b3[K].
+ */
+enum { BW_FEATURE_COUNT = 12, BW_MLP_HIDDEN = 64, BW_MLP_MAX_CLASSES = 16 };
+
+uint32_t bw_mlp_param_count(uint32_t classes);
+
+/* Features of the level about to run (identical to the device formula):
+ * frontier = vertices at the current depth, visited/edges_visited include
+ * the frontier. */
+void bw_bfs_features(uint64_t frontier_vertices, uint64_t frontier_edges,
+                     float log_degree_sum, float log_degree_sq_sum,
+                     float log_degree_max, uint64_t vertex_count,
+                     uint64_t edge_count, uint64_t visited,
+                     uint64_t edges_visited, uint32_t level, float out[12]);
+
+/*
+ * Per-level profile: at a sampled level each candidate variant runs from the
+ * same state (a candidate is undone by resetting the vertices it visited,
+ * which its emitted frontier queue lists) and is timed on the device; the
+ * traversal then continues.  Levels < 32 and every `sample_every`-th level
+ * (0 or 1 = all) are sampled; other levels run candidates[default_index]
+ * once and get level_ms = -1.  level_ms[level * K + k] and
+ * features[level * 12 + i] are filled for each level run (level_count).
+ */
+int bw_bfs_profile(bw_context *ctx, const bw_graph_view *g, uint32_t root,
+                   int32_t *levels, const int32_t *candidates, uint32_t K,
+                   uint32_t max_levels, uint32_t repeats,
+                   uint32_t sample_every, uint32_t default_index,
+                   float *level_ms, float *features, uint32_t *level_count,
+                   void *stream);
+
+typedef struct bw_mlp_train_config {
+    uint32_t steps;          /* optimiser steps */
+    uint32_t batch;          /* minibatch size (<= 64) */
+    float lr;                /* Adam step size */
+    float beta1, beta2, eps; /* Adam moments */
+    float weight_decay;
+    uint32_t reserved;
+    uint64_t seed;           /* minibatch sampling / initialisation */
+} bw_mlp_train_config;
+
+/* Initialise weights (seeded) and store the feature normalisation. */
+int bw_mlp_init(float *params, uint32_t classes, const float *mu,
+                const float *sd, uint64_t seed, void *stream);
+
+/*
+ * Train on n samples (device arrays): X[n][12] raw features, T[n][K] target
+ * distribution, W[n] sample weights (NULL = 1).  Loss: weighted soft-target
+ * cross-entropy.  One CTA runs every Adam step on the device.  loss_curve
+ * (host, optional) receives the mean minibatch loss of each block of
+ * steps/loss_points steps.
+ */
+int bw_mlp_train(bw_context *ctx, float *params, uint32_t classes,
+                 const float *X, const float *T, const float *W, uint32_t n,
+                 const bw_mlp_train_config *cfg, float *loss_curve,
+                 uint32_t loss_points, void *stream);
+
+/* Full-batch gradient of the mean loss (device grad[param_count]) and the
+ * loss value (host); used to check the backward pass. */
+int bw_mlp_gradient(bw_context *ctx, const float *params, uint32_t classes,
+                    const float *X, const float *T, const float *W,
+                    uint32_t n, float *grad, float *loss, void *stream);
+
+/* Softmax probabilities probs[n][K] (device). */
+int bw_mlp_predict(bw_context *ctx, const float *params, uint32_t classes,
+                   const float *X, uint32_t n, float *probs, void *stream);
+
+typedef struct bw_switch_config {
+    const float *params;        /* device MLP parameters */
+    uint32_t classes;           /* K */
+    int32_t fallback;           /* index into candidates */
+    const int32_t *candidates;  /* host array of K BFS variant ids */
+    float threshold;            /* below this top probability use fallback */
+    uint32_t reserved;
+} bw_switch_config;
+
+/*
+ * BFS whose every level runs the variant the MLP picks from that level's
+ * features (fallback below the confidence threshold).  BW_LOOP_GRAPH runs
+ * the prediction on the device inside the CUDA graph (a SWITCH conditional
+ * node selects the level kernel); BW_LOOP_HOST predicts on the host.  The
+ * depths are bit-identical to every fixed variant's; stats[level].variant
+ * records the choices.
+ */
+int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g,
+                       const bw_switch_config *sw, uint32_t root,
+                       int32_t *levels, int loop_mode, uint32_t max_levels,
+                       bw_bfs_result *result, bw_bfs_level_stats *stats,
+                       uint32_t stats_capacity, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,129 @@
+"""Learned variant switching on the GPU: features, MLP forward/backward
+against the float64 oracle, training, profiling, and the switched BFS
+(bit-exact depths, device and host prediction)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import belewitte_gb300 as bw
+import oracle
+from belewitte_gb300 import learn
+from oracle import mlp as mlp_oracle
+from tests.graphs import catalog, root_of
+
+pytestmark = pytest.mark.gpu
+K = len(learn.CANDIDATES)
+
+
+def _random_params(seed=3):
+    rng = np.random.default_rng(seed)
+    mu = rng.normal(size=12).astype(np.float32)
+    sd = rng.uniform(0.5, 2.0, size=12).astype(np.float32)
+    return learn.init_params(K, mu, sd, seed=seed)
+
+
+def _data(n, seed=5):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(size=(n, 12)).astype(np.float32) * 3
+    T = rng.dirichlet(np.ones(K) * 0.3, size=n).astype(np.float32)
+    W = rng.uniform(0.1, 3.0, size=n).astype(np.float32)
+    return X, T, W
+
+
+def test_forward_matches_oracle(ctx):
+    p = _random_params()
+    X, _, _ = _data(300)
+    got = learn.predict(ctx, p, X, K)
+    want, _ = mlp_oracle.forward(p.cpu().numpy(), X, K)
+    assert np.abs(got - want).max() < 2e-5
+
+
+def test_gradient_matches_oracle(ctx):
+    """The hand-written backward pass against the float64 oracle."""
+    p = _random_params(7)
+    X, T, W = _data(257, seed=9)
+    g, loss = learn.gradient(ctx, p, X, T, W)
+    want_loss, want = mlp_oracle.loss_and_grad(p.cpu().numpy(), X, T, W, K)
+    assert loss == pytest.approx(want_loss, rel=1e-4)
+    scale = np.abs(want).max()
+    assert np.abs(g - want).max() <= 1e-4 * scale + 1e-7
+    # unweighted form
+    g2, _ = learn.gradient(ctx, p, X, T, None)
+    _, want2 = mlp_oracle.loss_and_grad(p.cpu().numpy(), X, T, None, K)
+    assert np.abs(g2 - want2).max() <= 1e-4 * np.abs(want2).max() + 1e-7
+
+
+def test_training_learns_separable_rule(ctx):
+    """Labels that depend on two features: training must reach high accuracy."""
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(4000, 12)).astype(np.float32)
+    cls = (X[:, 0] > 0).astype(int) * 2 + (X[:, 3] > 0.5).astype(int)
+    T = np.zeros((len(X), K), np.float32)
+    T[np.arange(len(X)), cls] = 1.0
+    params, curve = learn.train(ctx, X, T, np.ones(len(X), np.float32), steps=3000, lr=3e-3)
+    assert curve[-1] < curve[0] * 0.3
+    acc = (learn.predict(ctx, params, X, K).argmax(1) == cls).mean()
+    assert acc > 0.95
+
+
+def test_features_host_equals_device(ctx):
+    h = catalog()["rmat14"][0]()
+    g = bw.DeviceGraph(h)
+    r = h.max_out_degree_vertex()
+    times, feats, levels = learn.profile_graph(ctx, g, r, sample_every=1)
+    lv, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, r)
+    assert np.array_equal(levels.cpu().numpy(), lv)
+    assert len(times) == len(cnt)
+    assert np.all(times > 0)
+    # recompute features on the host from the oracle's levels
+    deg = h.out_degrees().astype(np.float64)
+    visited, ev = 1, deg[r]
+    out = (C.c_float * 12)()
+    for L in range(len(cnt)):
+        front = lv == L
+        lg = np.log2(1 + deg[front])
+        bw.library().bw_bfs_features(int(front.sum()), int(deg[front].sum()), float(lg.sum()), float((lg * lg).sum()),
+                                     float(lg.max()) if front.any() else 0.0, h.vertex_count, h.edge_count,
+                                     visited, int(ev), L, out)
+        assert np.allclose(np.array(out), feats[L], rtol=1e-4, atol=1e-4), L
+        visited += int((lv == L + 1).sum())
+        ev += deg[lv == L + 1].sum()
+
+
+def _quick_predictor(ctx):
+    """A predictor trained on a few small graphs (fast)."""
+    recs = []
+    for spec in learn.catalogue(8, seed=11, max_scale=15, max_side=600):
+        g = spec.build()
+        t, f, _ = learn.profile_graph(ctx, g, learn.pick_root(g, spec.seed))
+        recs.append(learn.subsample_levels(t, f))
+    X, T, W = learn.build_dataset(recs)
+    params, _ = learn.train(ctx, X, T, W, steps=2000)
+    return learn.Predictor(params, learn.CANDIDATES, learn.fallback_variant(recs), 0.3), recs
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+def test_learned_bfs_bitexact(ctx, loop):
+    pred, _ = _quick_predictor(ctx)
+    for name in ["rmat14", "grid", "ba", "er", "star", "tiny", "isolated"]:
+        make, root = catalog()[name]
+        h = make()
+        g = bw.DeviceGraph(h)
+        r = root_of(h, root)
+        lv, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, r)
+        run = learn.run_learned(ctx, g, pred, r, loop=loop)
+        assert np.array_equal(run.levels.cpu().numpy(), lv), (name, loop)
+        assert [s["frontier_vertices"] for s in run.level_stats] == list(cnt)
+        allowed = {bw.bfs_variant_id(c) for c in learn.CANDIDATES}
+        assert all(s["variant"] in allowed for s in run.level_stats)
+
+
+def test_device_and_host_predictions_agree(ctx):
+    pred, _ = _quick_predictor(ctx)
+    h = catalog()["rmat14"][0]()
+    g = bw.DeviceGraph(h)
+    r = h.max_out_degree_vertex()
+    a = learn.run_learned(ctx, g, pred, r, loop="graph")
+    b = learn.run_learned(ctx, g, pred, r, loop="host")
+    assert [s["variant"] for s in a.level_stats] == [s["variant"] for s in b.level_stats]
