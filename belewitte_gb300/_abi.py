@@ -134,6 +134,8 @@ SIGNATURES = {
     "bw_bfs_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
                                      C.c_void_p, C.c_int, C.c_uint32, C.POINTER(BfsResult),
                                      C.POINTER(BfsLevelStats), C.c_uint32, C.c_void_p]),
+    "bw_bfs_run_noalloc": (C.c_int, [C.POINTER(GraphView), C.c_uint32, C.c_void_p, C.c_uint32,
+                                     C.POINTER(C.c_uint32), C.c_void_p]),
 }
 
 _lib = None

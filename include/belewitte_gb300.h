@@ -461,6 +461,31 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g,
                        bw_bfs_result *result, bw_bfs_level_stats *stats,
                        uint32_t stats_capacity, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free BFS                                                       */
+/* ------------------------------------------------------------------------ */
+/*
+ * No counterpart in the reference.  BFS (frontier-push) that allocates no
+ * memory: for callers that cannot allocate device memory while running,
+ * such as a serving process that reserves its HBM budget at start-up and
+ * forbids cudaMalloc on the request path (it can synchronise the device and
+ * fail under fragmentation), or a host application that loads this library
+ * under an allocator policy it does not own.  The caller passes the graph
+ * (forward CSR), the depth array (N int32, device) and a stream; the BFS
+ * scratch (frontier queues, hub-chunk queue, counters) is a fixed file-scope
+ * device array of about 9.2 MB that every GPU loading the library holds
+ * until exit.  Limits: at most 1,048,576 vertices and 16,777,216 edges;
+ * larger graphs return BW_ERR_TOO_LARGE.  The first call on a device looks up
+ * that array's device address (with the device current); make that first
+ * call before any stream capture.  Every call shares the one array and
+ * re-initialises it: calls that overlap on the GPU (other streams, other
+ * threads) race and must not be issued.  Depths are identical to
+ * bw_bfs_run(..., "frontier-push", ...); *level_count gets the levels run.
+ */
+int bw_bfs_run_noalloc(const bw_graph_view *g, uint32_t root, int32_t *levels,
+                       uint32_t max_levels, uint32_t *level_count,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif
