@@ -58,6 +58,10 @@ class PagerankResult(C.Structure):
                 ("device_ms", C.c_double)]
 
 
+class BatchResult(C.Structure):
+    _fields_ = [("units", C.c_uint64), ("traversed_edges", C.c_uint64), ("device_ms", C.c_double)]
+
+
 class MlpTrainConfig(C.Structure):
     _fields_ = [("steps", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("beta1", C.c_float),
                 ("beta2", C.c_float), ("eps", C.c_float), ("weight_decay", C.c_float), ("reserved", C.c_uint32),
@@ -134,6 +138,9 @@ SIGNATURES = {
     "bw_bfs_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
                                      C.c_void_p, C.c_int, C.c_uint32, C.POINTER(BfsResult),
                                      C.POINTER(BfsLevelStats), C.c_uint32, C.c_void_p]),
+    "bw_batch_run": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_int, C.c_void_p, C.c_uint32, C.c_void_p,
+                               C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                               C.POINTER(LaunchConfig), C.POINTER(BatchResult), C.c_void_p]),
     "bw_bfs_run_noalloc": (C.c_int, [C.POINTER(GraphView), C.c_uint32, C.c_void_p, C.c_uint32,
                                      C.POINTER(C.c_uint32), C.c_void_p]),
 }

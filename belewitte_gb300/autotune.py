@@ -1,0 +1,129 @@
+"""Launch-geometry autotuner for the BFS and PageRank variants.
+
+The reference fixes its geometry with Backend::computeDivision
+(Backend.cpp:52-70) and takes the virtual-warp width and chunk of the warp
+variants from -w/-c (ImplementationTemplate.hpp:431-436, defaults 32/32).
+This tuner times each variant on a graph over a small grid of choices --
+block size, grid size as a multiple of the SM count, and (warp variants)
+virtual-warp width and chunk -- on the device, and keeps the fastest per
+(algorithm, variant, graph shape class) in a JSON cache.  Results are
+identical for every configuration (BFS depths bit-exact, PageRank within
+the variant's tolerance), so tuning changes time only.
+"""
+from __future__ import annotations
+
+import itertools
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+
+from . import bfs, bfs_variant_names, pagerank, pagerank_variant_names
+
+CACHE = Path(__file__).resolve().parent / "data" / "autotune.json"
+
+BLOCKS = {"edge": [128, 256, 512], "vertex": [128, 256, 512], "warp": [128, 256, 512], "fixed": [256]}
+GRID_MULT = [2, 4, 8, 16]
+WARP = [(4, 32), (8, 64), (16, 64), (32, 32), (32, 128)]
+
+
+def shape_class(g) -> str:
+    """Coarse graph class: log2 vertices, log2 average degree, skew."""
+    deg = (g.fwd_vertices[1:] - g.fwd_vertices[:-1]).float()
+    avg = max(g.edge_count / max(g.vertex_count, 1), 1.0)
+    skew = float(deg.max().item()) / avg
+    return f"v{int(math.log2(max(g.vertex_count, 2)))}-d{int(math.log2(avg))}-s{int(math.log2(max(skew, 1)))}"
+
+
+def _kind(algorithm: str, name: str) -> str:
+    base = name
+    for suffix in ("-bulk", "-warpreduce", "-blockreduce"):
+        if base.endswith(suffix):
+            base = base[: -len(suffix)]
+    if base.startswith("frontier-") or base == "pull-segmented":
+        return "fixed"
+    if algorithm == "pagerank" and base in ("vertex-pull", "vertex-pull-nodiv"):
+        return "fixed"
+    if base in ("vertex-push-warp", "vertex-pull-warp", "vertex-pull-warp-nodiv"):
+        return "warp"
+    if base in ("edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list"):
+        return "edge"
+    return "vertex"
+
+
+def candidates(algorithm: str, name: str, sm_count: int):
+    kind = _kind(algorithm, name)
+    blocks = BLOCKS[kind]
+    if algorithm == "pagerank" and kind in ("edge", "vertex"):
+        blocks = [128, 256]                    # PageRank kernels are built for <= 256 threads
+    for blk, mult in itertools.product(blocks, GRID_MULT if kind != "fixed" else [0]):
+        grid = sm_count * mult if mult else 0
+        if kind == "warp":
+            for w, c in WARP:
+                if blk % w == 0:
+                    yield dict(block=blk, grid=grid, warp=w, chunk=c)
+        else:
+            yield dict(block=blk, grid=grid)
+
+
+def _time_bfs(ctx, g, name, root, cfg, repeats):
+    ts = [bfs(ctx, g, name, root, loop="graph", **cfg).device_ms for _ in range(repeats)]
+    return float(np.median(ts))
+
+
+def _time_pagerank(ctx, g, name, cfg, repeats, iterations):
+    ts = [pagerank(ctx, g, name, iterations, **cfg).device_ms for _ in range(repeats)]
+    return float(np.median(ts))
+
+
+def tune(ctx, g, algorithm: str, variants=None, *, root: int = 0, repeats: int = 3, iterations: int = 5,
+         cache: Path | None = CACHE, log=None):
+    """Tune `variants` on graph `g`; returns {variant: (config, ms)} and
+    updates the cache."""
+    names = variants or (bfs_variant_names() if algorithm == "bfs" else pagerank_variant_names())
+    cls = shape_class(g)
+    out = {}
+    for name in names:
+        best = None
+        for cfg in candidates(algorithm, name, ctx.sm_count):
+            try:
+                if algorithm == "bfs":
+                    ms = _time_bfs(ctx, g, name, root, cfg, repeats)
+                else:
+                    ms = _time_pagerank(ctx, g, name, cfg, repeats, iterations)
+            except Exception:
+                continue                         # e.g. shared memory limit for a warp config
+            if best is None or ms < best[1]:
+                best = (cfg, ms)
+        if best is None:
+            continue
+        out[name] = best
+        if log:
+            log(f"{algorithm} {name} {cls}: {best[0]} {best[1]:.3f} ms")
+    if cache is not None:
+        data = json.loads(cache.read_text()) if cache.exists() else {}
+        for name, (cfg, ms) in out.items():
+            data.setdefault(algorithm, {}).setdefault(name, {})[cls] = {"config": cfg, "ms": ms}
+        cache.parent.mkdir(parents=True, exist_ok=True)
+        cache.write_text(json.dumps(data, indent=1, sort_keys=True))
+    return out
+
+
+def lookup(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
+    """The tuned configuration for the nearest cached shape class (or {})."""
+    if not cache.exists():
+        return {}
+    entries = json.loads(cache.read_text()).get(algorithm, {}).get(name, {})
+    if not entries:
+        return {}
+    cls = shape_class(g)
+    if cls in entries:
+        return dict(entries[cls]["config"])
+
+    def dist(other: str) -> int:
+        a = [int(x[1:]) for x in cls.split("-")]
+        b = [int(x[1:]) for x in other.split("-")]
+        return sum(abs(x - y) for x, y in zip(a, b))
+    near = min(entries, key=dist)
+    return dict(entries[near]["config"])

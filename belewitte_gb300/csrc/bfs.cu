@@ -85,6 +85,7 @@ __global__ void k_bfs_init_side(int32_t *levels, uint64_t n, uint32_t root, uint
         ctl->visited = 1;
         ctl->traversed = 0;
         ctl->max_levels = max_levels;
+        ctl->skip = 0;
         if (outdeg) {
             const uint32_t d = outdeg[root];
             const float l = __log2f(1.0f + static_cast<float>(d));
@@ -110,8 +111,10 @@ __global__ void k_bfs_step(BfsCtl *ctl, LevelSlot *log, uint32_t log_cap,
     const LevelSlot s = ctl->slot[L % 3];
     if (log && static_cast<uint32_t>(L) < log_cap) log[L] = s;
     ctl->visited += s.frontier;
+    ctl->traversed += s.fedges;
     ctl->levels_done = static_cast<uint32_t>(L) + 1;
     ctl->depth = L + 1;
+    ctl->skip = 0;
     bool stop = s.frontier == 0;
     if (!stop && ctl->levels_done >= ctl->max_levels) {
         ctl->status = BW_ERR_LEVEL_LIMIT;
@@ -324,6 +327,8 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
     if (max_levels == 0) max_levels = static_cast<uint32_t>(std::min<uint64_t>(n + 1, 0xffffffffULL));
     Launch plan;
     BW_TRY(plan_launch(ctx, variant, side, cfg, &plan));
+    const bool cluster_path = variant == V_FRONTIER_PUSH;
+    if (cluster_path) BW_TRY(ensure_outdeg(ctx, g, s));   // frontier edge volumes gate the cluster path
     LevelSlot *log = nullptr;
     const uint32_t log_cap = stats ? std::min(stats_cap, max_levels) : 0;
     if (log_cap) BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
@@ -357,6 +362,13 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
         e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
             BfsArgs a = make_args(ctx, g, levels, -1, cfg);
+            if (cluster_path) {
+                // small frontiers: the cluster kernel runs many levels per launch
+                a.skip_check = 1;
+                a.log = log;
+                a.log_cap = log_cap;
+                bfs_cluster_kernel(side)<<<CLUSTER_CTAS, CLUSTER_THREADS, 0, cap>>>(a);
+            }
             plan.k<<<plan.grid, plan.block, plan.smem, cap>>>(a);
             if (plan.k2) plan.k2<<<plan.grid, plan.block, 0, cap>>>(a);
             k_bfs_step<<<1, 32, 0, cap>>>(ctx->bfs_ctl, log, log_cap, handle);
@@ -378,7 +390,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
     }
 
     k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels,
-                                                     side ? ctx->outdeg : nullptr);
+                                                     (side || cluster_path) ? ctx->outdeg : nullptr);
     BW_CUDA(cudaGetLastError());
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
     BW_CUDA(cudaGraphLaunch(exec, s));

@@ -117,6 +117,13 @@ __device__ __forceinline__ bool relax(int32_t *levels, uint32_t v, int32_t nd)
     return levels[v] > nd && atomicMin(&levels[v], nd) > nd;
 }
 
+// Warp-reduce an out-edge count into slot->fedges (every lane must call).
+__device__ __forceinline__ void flush_edges(LevelSlot *s, unsigned long long fe)
+{
+    for (int o = 16; o > 0; o >>= 1) fe += __shfl_xor_sync(FULL_MASK, fe, o);
+    if ((threadIdx.x & 31) == 0 && fe) atomicAdd(&s->fedges, fe);
+}
+
 __device__ __forceinline__ uint64_t gtid()
 { return blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; }
 __device__ __forceinline__ uint64_t gthreads()
@@ -358,6 +365,7 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
 {
     __shared__ uint32_t s_excl[8][32];
     __shared__ uint32_t s_start[8][32];
+    if (a.skip_check && *((volatile uint32_t *) &a.ctl->skip)) return;
     const int32_t depth = level_depth(a), nd = depth + 1;
     LevelSlot *slot = &a.ctl->slot[depth % 3];
     if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
@@ -369,6 +377,7 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
     Side<SIDE> side;
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    unsigned long long fe = 0;   // next-frontier out-edges (cluster-path gating)
 
     for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
         const uint64_t i = t + lane;
@@ -405,17 +414,20 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
                 cnt.hit(&slot->frontier);
                 queue_append(qnext, &slot->qlen, u);
                 if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
+                else if (a.skip_check) fe += a.outdeg[u];
             }
         }
         __syncwarp();
     }
     cnt.finish(&slot->frontier);
     side.finish(slot);
+    if constexpr (!SIDE) flush_edges(slot, fe);
 }
 
 template<bool SIDE>
 __global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
 {
+    if (a.skip_check && *((volatile uint32_t *) &a.ctl->skip)) return;
     const int32_t depth = level_depth(a), nd = depth + 1;
     LevelSlot *slot = &a.ctl->slot[depth % 3];
     uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
@@ -425,6 +437,7 @@ __global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
     Side<SIDE> side;
     const unsigned lane = threadIdx.x & 31;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    unsigned long long fe = 0;
     for (uint64_t c = warp; c < chunks; c += warps) {
         const uint2 h = a.heavy[c];
         const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
@@ -434,11 +447,13 @@ __global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
                 cnt.hit(&slot->frontier);
                 queue_append(qnext, &slot->qlen, u);
                 if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
+                else if (a.skip_check) fe += a.outdeg[u];
             }
         }
     }
     cnt.finish(&slot->frontier);
     side.finish(slot);
+    if constexpr (!SIDE) flush_edges(slot, fe);
 }
 
 // ---------------------------------------------------------------------------
@@ -500,6 +515,143 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
     }
     cnt.finish(&slot->frontier);
     side.finish(slot);
+}
+
+// ---------------------------------------------------------------------------
+// frontier-push, small-frontier path (device loop only): one cluster of
+// CLUSTER_CTAS blocks keeps expanding levels, separated by cluster barriers,
+// while the frontier stays at or below CLUSTER_CAP vertices -- the
+// high-diameter case (2-D grids, BFS tails) where one launch per level would
+// dominate.  It does the per-level bookkeeping of the device-loop step for
+// every level but the last, sets ctl->skip so the regular frontier-push
+// kernels of the same loop iteration return at once, and leaves the last
+// level to the step kernel.  A frontier above the cap at entry is left to
+// the regular kernels.  Data written by other CTAs of the cluster (queues,
+// hub chunks, counters) is read through L2 (L1 is not coherent).
+// ---------------------------------------------------------------------------
+constexpr uint32_t CLUSTER_CAP = 65536;            // frontier vertices
+constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;   // frontier out-edges
+
+template<bool SIDE>
+__global__ void __cluster_dims__(CLUSTER_CTAS, 1, 1) __launch_bounds__(CLUSTER_THREADS)
+k_bfs_cluster(BfsArgs a)
+{
+    __shared__ uint32_t s_excl[CLUSTER_THREADS / 32][32];
+    __shared__ uint32_t s_start[CLUSTER_THREADS / 32][32];
+    cg::cluster_group cl = cg::this_cluster();
+    BfsCtl *ctl = a.ctl;
+    const unsigned rank = cl.block_rank();
+    const bool leader = rank == 0 && threadIdx.x == 0;
+    int32_t L = *((volatile int32_t *) &ctl->depth);
+    const uint32_t max_levels = *((volatile uint32_t *) &ctl->max_levels);
+    uint32_t qlen = *((volatile uint32_t *) &ctl->slot[(L + 2) % 3].qlen);
+    const unsigned long long fedges = *((volatile unsigned long long *) &ctl->slot[(L + 2) % 3].fedges);
+    // same values in every block: a large or edge-heavy frontier is left to
+    // the full-GPU kernels
+    if (qlen == 0 || qlen > CLUSTER_CAP || fedges > CLUSTER_EDGE_CAP) return;
+    int32_t *lv = a.levels;
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t warp = uint64_t(rank) * (CLUSTER_THREADS / 32) + wib;
+    const uint64_t warps = uint64_t(CLUSTER_CTAS) * (CLUSTER_THREADS / 32);
+    for (;;) {
+        const int32_t nd = L + 1;
+        LevelSlot *slot = &ctl->slot[L % 3];
+        if (leader) reset_slot(&ctl->slot[(L + 1) % 3]);
+        const uint32_t *qin = (L & 1) ? a.q1 : a.q0;
+        uint32_t *qnext = (L & 1) ? a.q0 : a.q1;
+        Counter<RED_WARP> cnt;
+        Side<SIDE> side;
+        unsigned long long fe = 0;
+        for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
+            const uint64_t i = t + lane;
+            uint32_t v = 0, s = 0, d = 0;
+            if (i < qlen) {
+                v = __ldcg(qin + i);
+                s = a.fwd_v[v];
+                d = a.fwd_v[v + 1] - s;
+            }
+            if (d > HEAVY_DEGREE) {
+                const uint32_t chunks = (d + HUB_CHUNK - 1) / HUB_CHUNK;
+                const uint32_t base = atomicAdd(&slot->heavy, chunks);
+                for (uint32_t c = 0; c < chunks; c++) a.heavy[base + c] = make_uint2(v, s + c * HUB_CHUNK);
+                d = 0;
+            }
+            uint32_t incl = d;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
+                if (lane >= static_cast<unsigned>(o)) incl += y;
+            }
+            const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+            s_excl[wib][lane] = incl - d;
+            s_start[wib][lane] = s;
+            __syncwarp();
+            for (uint32_t k = lane; k < total; k += 32) {
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
+                }
+                const uint32_t u = __ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo]));
+                if (relax(lv, u, nd)) {
+                    cnt.hit(&slot->frontier);
+                    queue_append(qnext, &slot->qlen, u);
+                    if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
+                    else fe += a.outdeg[u];
+                }
+            }
+            __syncwarp();
+        }
+        cnt.finish(&slot->frontier);
+        side.finish(slot);
+        if constexpr (!SIDE) flush_edges(slot, fe);
+        cl.sync();
+        const uint32_t chunks = __ldcg(&slot->heavy);
+        if (chunks) {                                      // hub chunks: a second phase
+            Counter<RED_WARP> cnt2;
+            Side<SIDE> side2;
+            unsigned long long fe2 = 0;
+            for (uint64_t c = warp; c < chunks; c += warps) {
+                const uint2 h = __ldcg(a.heavy + c);
+                const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
+                for (uint32_t i = h.y + lane; i < end; i += 32) {
+                    const uint32_t u = __ldg(a.fwd_e + i);
+                    if (relax(lv, u, nd)) {
+                        cnt2.hit(&slot->frontier);
+                        queue_append(qnext, &slot->qlen, u);
+                        if constexpr (SIDE) side2.visit(a, nullptr, nullptr, u);
+                        else fe2 += a.outdeg[u];
+                    }
+                }
+            }
+            cnt2.finish(&slot->frontier);
+            side2.finish(slot);
+            if constexpr (!SIDE) flush_edges(slot, fe2);
+            cl.sync();
+        }
+        const uint32_t f = __ldcg(&slot->qlen);
+        const unsigned long long fnext = __ldcg(&slot->fedges);
+        if (f == 0 || f > CLUSTER_CAP || fnext > CLUSTER_EDGE_CAP || static_cast<uint32_t>(L) + 2 > max_levels) {
+            if (leader) ctl->skip = 1;                     // level L is left to the step kernel
+            return;
+        }
+        if (leader) {                                      // the step kernel's bookkeeping for level L
+            LevelSlot sl;
+            sl.frontier = __ldcg(&slot->frontier);
+            sl.qlen = f;
+            sl.fedges = __ldcg(&slot->fedges);
+            sl.lsum = __ldcg(&slot->lsum);
+            sl.lsq = __ldcg(&slot->lsq);
+            sl.lmax_bits = __ldcg(&slot->lmax_bits);
+            sl.heavy = static_cast<uint32_t>(ctl->variant);
+            if (a.log && static_cast<uint32_t>(L) < a.log_cap) a.log[L] = sl;
+            ctl->visited += sl.frontier;
+            ctl->traversed += sl.fedges;
+            ctl->levels_done = static_cast<uint32_t>(L) + 1;
+            ctl->depth = L + 1;
+        }
+        qlen = f;
+        L++;
+    }
 }
 
 }  // namespace bw

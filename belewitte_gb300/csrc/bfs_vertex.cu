@@ -32,6 +32,9 @@ BfsKernelFn bfs_frontier_push_kernel(bool side)
 BfsKernelFn bfs_hub_kernel(bool side)
 { return side ? k_bfs_hub_chunks<true> : k_bfs_hub_chunks<false>; }
 
+BfsKernelFn bfs_cluster_kernel(bool side)
+{ return side ? k_bfs_cluster<true> : k_bfs_cluster<false>; }
+
 BfsKernelFn bfs_frontier_pull_kernel(bool side)
 { return side ? k_bfs_frontier_pull<true> : k_bfs_frontier_pull<false>; }
 

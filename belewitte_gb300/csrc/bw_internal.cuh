@@ -61,7 +61,8 @@ struct BfsCtl {
     unsigned long long visited;   // running totals (device loop)
     unsigned long long traversed;
     uint32_t max_levels;
-    uint32_t pad[3];
+    uint32_t skip;                // the cluster kernel already ran this level
+    uint32_t pad[2];
 };
 
 struct BfsArgs {
@@ -76,6 +77,9 @@ struct BfsArgs {
     uint2 *heavy;                 // hub chunk queue {vertex, first edge}
     int32_t depth;                // >= 0: this level; < 0: read ctl->depth
     uint32_t warp_size, chunk_size;
+    uint32_t skip_check;          // device loop with the cluster path: honour ctl->skip
+    LevelSlot *log;               // device-loop level log (cluster path)
+    uint32_t log_cap;
 };
 
 // ---------------------------------------------------------------------------
@@ -143,6 +147,9 @@ BfsKernelFn bfs_vertex_kernel(int family, int reduction, bool side);
 BfsKernelFn bfs_frontier_push_kernel(bool side);
 BfsKernelFn bfs_hub_kernel(bool side);
 BfsKernelFn bfs_frontier_pull_kernel(bool side);
+BfsKernelFn bfs_cluster_kernel(bool side);   // 8-CTA cluster, CLUSTER_CTAS blocks of 1024 threads
+constexpr unsigned CLUSTER_CTAS = 8;
+constexpr unsigned CLUSTER_THREADS = 1024;
 
 // Reference Backend::computeDivision (Backend.cpp:52-70).
 void compute_division(uint64_t count, uint32_t sm, uint32_t max_tpb,

@@ -415,6 +415,7 @@ __global__ void k_bfs_step_learned(BfsCtl *ctl, LevelSlot *log, uint32_t log_cap
     ctl->traversed += s.fedges;
     ctl->levels_done = static_cast<uint32_t>(L) + 1;
     ctl->depth = L + 1;
+    ctl->skip = 0;
     bool stop = s.frontier == 0;
     if (!stop && ctl->levels_done >= ctl->max_levels) {
         ctl->status = BW_ERR_LEVEL_LIMIT;
@@ -742,9 +743,21 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
         cudaGraphNode_t snode;
         if ((e = cudaGraphAddNode(&snode, body, &pnode, nullptr, 1, &sp)) != cudaSuccess) { fail(e, "switch node"); break; }
         BfsArgs a = bfs_args(ctx, g, levels, -1, nullptr);
+        a.skip_check = 1;
+        a.log = log;
+        a.log_cap = log_cap;
         for (uint32_t k = 0; k < K && rc == BW_OK; k++) {
             cudaGraph_t kb = sp.conditional.phGraph_out[k];
             void *kargs[] = {&a};
+            cudaGraphNode_t first = nullptr;
+            if (sw->candidates[k] == 32) {      // frontier-push: small-frontier cluster path first
+                cudaKernelNodeParams cp = {};
+                cp.func = reinterpret_cast<void *>(bfs_cluster_kernel(true));
+                cp.gridDim = dim3(CLUSTER_CTAS);
+                cp.blockDim = dim3(CLUSTER_THREADS);
+                cp.kernelParams = kargs;
+                if ((e = cudaGraphAddKernelNode(&first, kb, nullptr, 0, &cp)) != cudaSuccess) { fail(e, "cluster node"); break; }
+            }
             cudaKernelNodeParams lp = {};
             lp.func = reinterpret_cast<void *>(plans[k].k);
             lp.gridDim = dim3(plans[k].grid);
@@ -752,7 +765,9 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             lp.sharedMemBytes = static_cast<unsigned>(plans[k].smem);
             lp.kernelParams = kargs;
             cudaGraphNode_t n1;
-            if ((e = cudaGraphAddKernelNode(&n1, kb, nullptr, 0, &lp)) != cudaSuccess) { fail(e, "level node"); break; }
+            if ((e = cudaGraphAddKernelNode(&n1, kb, first ? &first : nullptr, first ? 1 : 0, &lp)) != cudaSuccess) {
+                fail(e, "level node"); break;
+            }
             if (plans[k].k2) {
                 cudaKernelNodeParams lp2 = lp;
                 lp2.func = reinterpret_cast<void *>(plans[k].k2);

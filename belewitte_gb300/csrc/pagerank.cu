@@ -22,6 +22,7 @@
 #include <cstring>
 #include <cooperative_groups.h>
 
+#include "bw_consolidate.h"
 #include "bw_internal.cuh"
 
 namespace bw {
@@ -81,10 +82,17 @@ __device__ __forceinline__ uint64_t gthreads() { return uint64_t(gridDim.x) * bl
 // -- a double base term (computed once: IEEE division is correctly rounded,
 // so the host value is the one the reference computes per vertex), a float
 // product, one double addition and the rounding to float.
+// The double addition and the rounding to float are done in integer
+// arithmetic (bw_consolidate.h): bit-identical to the FP64 instructions,
+// which GB300 issues at a small fraction of the FP32 rate.
 __device__ __forceinline__ float consolidate_div(float acc, double base)
 {
     const float scaled = __fmul_rn(DAMPING, acc);
-    return __double2float_rn(__dadd_rn(base, static_cast<double>(scaled)));
+    bool ok;
+    const uint32_t r = bwcons::add_round_bits(static_cast<uint64_t>(__double_as_longlong(base)),
+                                              __float_as_uint(scaled), ok);
+    if (ok) return __uint_as_float(r);
+    return __double2float_rn(__dadd_rn(base, static_cast<double>(scaled)));   // outside the emulated domain
 }
 
 __device__ __forceinline__ float nodiv_base(uint64_t n)

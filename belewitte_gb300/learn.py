@@ -81,17 +81,18 @@ def catalogue(count: int, seed: int, max_scale: int = 23, max_side: int = 4096) 
             a = float(rng.uniform(0.45, 0.70))
             rest = 1.0 - a
             b = c = round(rest * 0.38, 4)
-            out.append(GraphSpec("rmat", dict(scale=int(rng.integers(16, max_scale + 1)), edge_factor=16,
+            lo = min(16, max_scale)
+            out.append(GraphSpec("rmat", dict(scale=int(rng.integers(lo, max_scale + 1)), edge_factor=16,
                                               a=round(a, 4), b=b, c=c), s))
         elif fam == "grid":
-            side = int(round(2 ** rng.uniform(math.log2(512), math.log2(max_side))))
+            side = int(round(2 ** rng.uniform(math.log2(min(512, max_side)), math.log2(max_side))))
             out.append(GraphSpec("grid", dict(side=side), s))
         elif fam == "er":
-            n = int(2 ** rng.uniform(16, 22))
+            n = int(2 ** rng.uniform(min(16, max_scale), min(22, max_scale + 1)))
             deg = float(2 ** rng.uniform(2, 6))
             out.append(GraphSpec("er", dict(n=n, m=int(n * deg / 2)), s))
         else:
-            n = int(2 ** rng.uniform(16, 22))
+            n = int(2 ** rng.uniform(min(16, max_scale), min(22, max_scale + 1)))
             out.append(GraphSpec("ba", dict(n=n, m=int(2 ** rng.uniform(1, 5))), s))
     return out
 

@@ -1,28 +1,40 @@
-"""Benchmark: PageRank GTEPS per iteration on one GB300.
+"""Benchmark: GTEPS on one GB300 (PageRank per iteration; BFS learned switch).
 
-Workload (N=1 line): PageRank, FP32, damping 0.85, 1/N init, 30 fixed
-iterations on a seeded R-MAT graph, scale 22 (4,194,304 vertices, edge
-factor 16, a/b/c/d = 0.57/0.19/0.19/0.05, self-loops and duplicates
-removed), the configuration the reference's PageRank metric is quoted on.
-A step is one full 30-iteration PageRank over the device-resident graph.
+Headline line (N=1): PageRank, FP32, damping 0.85, 1/N init, 30 fixed
+iterations on a seeded R-MAT graph of scale 22 (4,194,304 vertices, edge
+factor 16, a/b/c/d = 0.57/0.19/0.19/0.05, self-loops and duplicates removed),
+the PageRank configuration the metric is quoted on.  A step is one full
+30-iteration PageRank over the device-resident graph with the fastest
+PageRank variant (chosen by a short on-device sweep, reported as `variant`);
 GTEPS = edges x iterations / time.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+The same JSON line carries:
+  * learned_switch: BFS on the symmetrised R-MAT scale-24 graph from 16 seeded
+    sources of the giant component -- the learned per-level switch (shipped
+    predictor, device-side decisions in a CUDA graph) against every fixed
+    candidate variant; depths are checked identical.
+  * batched: many graphs (BFS + 20-iteration PageRank each) and many BFS
+    sources, each in one persistent launch.
+  * roofline of the dominant PageRank kernel, e2e through the C ABI with
+    host buffers, the CPU baseline, clocks during the timed region.
 
-N > 1 (launched with torch.distributed.run): the path does not shard a
-single graph, so every rank runs an independent replica (weak scaling).
-`--impl reference` times the CPU restatement of the reference's PageRank
-(vertex-pull + consolidateRank, OpenMP over all host cores) on a bounded
-sample of the same workload.
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --case pagerank:VARIANT:rmat22|er   (small profiling case)
+  python bench.py --case bfs:VARIANT:rmat22            (small profiling case)
+
+N > 1 (torch.distributed.run): the path does not shard one graph, so each
+rank runs an independent replica (weak scaling).  --impl reference times the
+CPU restatement of the reference's PageRank (vertex-pull + consolidateRank,
+OpenMP on all host cores) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
 import subprocess
-import sys
 import threading
 import time
 
@@ -30,14 +42,11 @@ import numpy as np
 
 METRIC = "GTEPS (BFS, PageRank/iter) on 1 GB300: learned-switched vs best fixed variant"
 SCALE, EDGE_FACTOR, SEED, ITERATIONS = 22, 16, 22, 30
-HEADLINE_VARIANT = "pull-segmented"
+BFS_SCALE, BFS_SEED, BFS_SOURCES = 24, 24, 16
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
 class ClockSampler:
@@ -48,25 +57,20 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu: int):
-        self.gpu = gpu
-        self.proc = None
-        self.lines: list[str] = []
-        self._t = None
+        self.gpu, self.proc, self.lines, self._t = gpu, None, [], None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t = threading.Thread(target=lambda: [self.lines.append(x.strip()) for x in self.proc.stdout],
+                                       daemon=True)
             self._t.start()
+            time.sleep(0.3)
         except OSError:
             self.proc = None
         return self
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
 
     def __exit__(self, *exc):
         if self.proc:
@@ -95,8 +99,7 @@ class ClockSampler:
                     reasons.add(name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def _measured_peak():
@@ -107,13 +110,167 @@ def _measured_peak():
         return 6800.0, "fallback"
 
 
+FUSED = ("vertex-pull", "vertex-pull-warp", "vertex-pull-nodiv", "vertex-pull-warp-nodiv", "pull-segmented")
+ITEM_LISTS = ("vertex-pull", "vertex-pull-nodiv", "pull-segmented")
+DOMINANT = {"pull-segmented": "k_pr_pull_items", "vertex-pull": "k_pr_pull_items", "vertex-pull-nodiv": "k_pr_pull_items",
+            "vertex-pull-warp": "k_pr_vertex_pull_warp", "vertex-pull-warp-nodiv": "k_pr_vertex_pull_warp",
+            "vertex-push": "k_pr_vertex_push", "vertex-push-warp": "k_pr_vertex_push_warp"}
+
+
 def pagerank_launches(variant: str, iterations: int) -> int:
     """Kernels of ours one bw_pagerank_run launches (memsets not counted)."""
-    fused = variant in ("vertex-pull", "vertex-pull-warp", "vertex-pull-nodiv", "vertex-pull-warp-nodiv",
-                        "pull-segmented")
     deg = 0 if variant in ("vertex-push", "vertex-push-warp") else 1
-    seg = 3 if variant == "pull-segmented" else 0
-    return deg + seg + 1 + iterations * (1 if fused else 2)
+    seg = 3 if variant in ITEM_LISTS else 0
+    return deg + seg + 1 + iterations * (1 if variant in FUSED else 2)
+
+
+def alg_bytes(variant: str, n: int, m: int) -> int:
+    """Compulsory bytes of one PageRank iteration."""
+    if variant.startswith(("edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list")):
+        return 8 * m + 12 * n
+    return 4 * m + 16 * n + 4
+
+
+def pick_pagerank_variant(ctx, g, names):
+    """Fastest variant of the div class on this graph (short on-device sweep)."""
+    import belewitte_gb300 as bw
+    best = None
+    for v in names:
+        if "nodiv" in v:
+            continue                           # different semantics: not interchangeable
+        t = min(bw.pagerank(ctx, g, v, 5).device_ms for _ in range(2))
+        if best is None or t < best[1]:
+            best = (v, t)
+    return best[0]
+
+
+def bfs_learned_vs_fixed(ctx, dev):
+    """Learned switch vs fixed candidates on the symmetrised R-MAT-24 graph."""
+    import torch
+
+    import belewitte_gb300 as bw
+    from belewitte_gb300 import learn
+    g = bw.DeviceGraph.generate("rmat", scale=BFS_SCALE, edge_factor=EDGE_FACTOR, seed=BFS_SEED, symmetrise=True,
+                                device=dev, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR | bw.REP_FWD_EL | bw.REP_FWD_ST)
+    pred = learn.load_predictor(device=dev)
+    deg = g.fwd_vertices[1:] - g.fwd_vertices[:-1]
+    hub = int(torch.argmax(deg).item())
+    reach = torch.nonzero(bw.bfs(ctx, g, "frontier-pull", hub).levels != bw.INF).flatten().cpu().numpy()
+    sources = [int(x) for x in np.random.default_rng(BFS_SEED).choice(reach, BFS_SOURCES, replace=False)]
+    fixed = ["edge-list-bulk", "struct-edge-list-bulk", "frontier-push", "frontier-pull", "vertex-pull-warp-bulk"]
+    times = {k: 0.0 for k in ["learned"] + fixed}
+    edges = 0
+    for r in sources:
+        learn.run_learned(ctx, g, pred, r, loop="graph", stats=False)          # warm-up of this source
+        run = learn.run_learned(ctx, g, pred, r, loop="graph", stats=False)
+        times["learned"] += run.device_ms
+        edges += run.traversed_edges
+        for v in fixed:
+            rr = bw.bfs(ctx, g, v, r, loop="graph")
+            if not torch.equal(rr.levels, run.levels):
+                raise AssertionError(f"BFS depths of {v} differ from the learned run")
+            times[v] += rr.device_ms
+    best = min(fixed, key=lambda v: times[v])
+    out = {"workload": f"BFS R-MAT scale {BFS_SCALE} symmetrised (seed {BFS_SEED}), {BFS_SOURCES} seeded sources",
+           "vertices": g.vertex_count, "edges": g.edge_count,
+           "learned_gteps": round(edges / (times["learned"] * 1e-3) / 1e9, 2),
+           "best_fixed_variant": best, "best_fixed_gteps": round(edges / (times[best] * 1e-3) / 1e9, 2),
+           "speedup_vs_best_fixed": round(times[best] / times["learned"], 3),
+           "ms_total": {k: round(v, 3) for k, v in times.items()}, "depths_identical": True}
+    del g
+    torch.cuda.empty_cache()
+    return out
+
+
+def batched(ctx, dev, graphs: int):
+    import torch
+
+    import belewitte_gb300 as bw
+    from belewitte_gb300 import batch
+    out = {}
+    t0 = time.time()
+    specs = batch.workload_a_specs(graphs, seed=5)
+    gs = [bw.DeviceGraph.generate("rmat", scale=s["scale"], edge_factor=s["edge_factor"], seed=s["seed"],
+                                  device=dev) for s in specs]
+    packed = batch.pack(gs, device=dev)
+    del gs
+    gen_s = time.time() - t0
+    batch.run_graphs(ctx, packed, pr_iterations=20)                     # warm-up
+    _, _, res = batch.run_graphs(ctx, packed, pr_iterations=20)
+    out["graphs"] = {"workload": f"{graphs} R-MAT graphs, 2^10..2^18 vertices, edge factor 8-32; "
+                                 "BFS from each max-degree vertex + 20 PageRank iterations, one persistent launch",
+                     "vertices": packed.vertex_count, "edges": packed.edge_count, "ms": round(res.device_ms, 3),
+                     "gteps": round((res.traversed_edges + 20 * packed.edge_count) / (res.device_ms * 1e-3) / 1e9, 2),
+                     "generation_s": round(gen_s, 1)}
+    del packed
+    torch.cuda.empty_cache()
+    g = bw.DeviceGraph.generate("rmat", scale=20, edge_factor=16, seed=20, symmetrise=True, device=dev)
+    reach = torch.nonzero(bw.bfs(ctx, g, "frontier-pull", 0).levels != bw.INF).flatten().cpu().numpy()
+    srcs = np.random.default_rng(20).choice(reach, 1024, replace=False)
+    batch.run_sources(ctx, g, srcs[:64])
+    levels, res = batch.run_sources(ctx, g, srcs)
+    out["sources"] = {"workload": "1024 BFS sources on R-MAT scale 20 (symmetrised), one persistent launch",
+                      "ms": round(res.device_ms, 3), "gteps": round(res.traversed_edges / (res.device_ms * 1e-3) / 1e9, 2)}
+    del levels, g
+    torch.cuda.empty_cache()
+    return out
+
+
+class HostToDevice:
+    """The e2e leg: a caller holding the CSR in pinned host memory copies it
+    to preallocated device buffers every step and derives the edge-list /
+    struct-edge-list arrays the variant reads on the device (as
+    DeviceGraph does), then calls bw_pagerank_run through the C ABI."""
+
+    def __init__(self, host, variant, n, m, dev):
+        import torch
+        fwd = variant in ("vertex-push", "vertex-push-warp") or variant.startswith(("edge-list", "struct-edge-list"))
+        side = "fwd" if fwd else "rev"
+        self.side, self.n, self.m = side, n, m
+        self.el = variant.startswith(("edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list"))
+        self.st = "struct" in variant
+        self.host = {k: torch.from_numpy(host[f"{side}_{k}"].view(np.int32)).pin_memory()
+                     for k in ("vertices", "edges")}
+        self.dev = {k: torch.empty_like(v, device=f"cuda:{dev}") for k, v in self.host.items()}
+        self.in_edges = torch.empty(max(m, 1), dtype=torch.int32, device=f"cuda:{dev}") if self.el else None
+        self.struct = torch.empty(2 * max(m, 1), dtype=torch.int32, device=f"cuda:{dev}") if self.st else None
+        self.h2d_bytes = int(sum(v.numel() * 4 for v in self.host.values()))
+
+    def upload(self, stream):
+        from belewitte_gb300 import _abi
+        import belewitte_gb300 as bw
+        lib, sp = bw.library(), C.c_void_p(stream.cuda_stream)
+        for k in self.host:
+            self.dev[k].copy_(self.host[k], non_blocking=True)
+        off, adj = self.dev["vertices"].data_ptr(), self.dev["edges"].data_ptr()
+        inn = st = 0
+        if self.el:
+            inn = self.in_edges.data_ptr()
+            bw.check(lib.bw_expand_edge_list(C.c_void_p(off), self.n, self.m, C.c_void_p(inn), sp), "expand")
+        if self.st:
+            st = self.struct.data_ptr()
+            bw.check(lib.bw_build_struct_edges(C.c_void_p(inn), C.c_void_p(adj), self.m, C.c_void_p(st), sp),
+                     "struct")
+        if self.side == "fwd":
+            v = _abi.GraphView(self.n, self.m, off, adj, 0, 0, inn, 0, st, 0)
+        else:
+            v = _abi.GraphView(self.n, self.m, 0, 0, off, adj, 0, inn, 0, st)
+
+        class _View:
+            vertex_count, edge_count, view = self.n, self.m, v
+        return _View()
+
+
+def cpu_baseline(host, n, m, iterations):
+    import oracle
+    threads = os.cpu_count() or 1
+    deg = np.diff(host["fwd_vertices"].astype(np.int64)).astype(np.uint32)
+    t = time.perf_counter()
+    oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], iterations, deg=deg, threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": round(m * iterations / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"{iterations} of {ITERATIONS} iterations of the same R-MAT-{SCALE} PageRank "
+                      f"(vertex-pull + consolidateRank restated, OpenMP), {dt:.2f} s"}
 
 
 def run_ours(args):
@@ -121,6 +278,7 @@ def run_ours(args):
     import torch.distributed as dist
 
     import belewitte_gb300 as bw
+    from belewitte_gb300 import _abi
 
     ws, rank, local = _dist()
     if ws > 1:
@@ -130,11 +288,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     ctx = bw.Context(dev)
     stream = torch.cuda.current_stream()
-    g = bw.DeviceGraph.generate("rmat", scale=SCALE, edge_factor=EDGE_FACTOR, seed=SEED, device=dev,
-                                reps=bw.REP_FWD_CSR | bw.REP_REV_CSR)
+    g = bw.DeviceGraph.generate("rmat", scale=SCALE, edge_factor=EDGE_FACTOR, seed=SEED, device=dev, reps=63)
     n, m = g.vertex_count, g.edge_count
+    variant = args.variant or pick_pagerank_variant(ctx, g, bw.pagerank_variant_names())
     ranks = torch.empty(n, dtype=torch.float32, device=f"cuda:{dev}")
-    variant = args.variant
 
     # ---- device-resident timed region ------------------------------------
     for _ in range(args.warmup):
@@ -162,48 +319,42 @@ def run_ours(args):
     ms_per_step = ms / args.steps
     value = ws * m * ITERATIONS / (ms_per_step * 1e-3) / 1e9
 
-    # ---- roofline of the dominant kernel (one launch = one iteration) -----
-    kernel_ms = float(np.mean(iter_ms))
-    alg_bytes = 4 * m + 16 * n + 4              # CSR-pull compulsory bytes per iteration
+    kernel_ms = float(np.median(iter_ms))
+    ab = alg_bytes(variant, n, m)
     peak, peak_kind = _measured_peak()
-    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    achieved = ab / (kernel_ms * 1e-3) / 1e9
 
     # ---- end to end through the C ABI with host buffers ----------------------
     host = g.to_host_arrays()
-    rv = torch.from_numpy(host["rev_vertices"].view(np.int32)).pin_memory()
-    re = torch.from_numpy(host["rev_edges"].view(np.int32)).pin_memory()
+    e2e = HostToDevice(host, variant, n, m, dev)
     out_host = torch.empty(n, dtype=torch.float32).pin_memory()
-    d_rv = torch.empty_like(rv, device=f"cuda:{dev}")
-    d_re = torch.empty_like(re, device=f"cuda:{dev}")
-    import ctypes as C
-    from belewitte_gb300 import _abi
-    view = _abi.GraphView(n, m, 0, 0, d_rv.data_ptr(), d_re.data_ptr(), 0, 0, 0, 0)
-
-    class _G:                                   # a DeviceGraph-shaped view over the copies
-        vertex_count, edge_count = n, m
-    eg = _G()
-    eg.view = view
     e2e_times = []
     for i in range(args.warmup + args.steps):
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        d_rv.copy_(rv, non_blocking=True)
-        d_re.copy_(re, non_blocking=True)
-        bw.pagerank(ctx, eg, variant, ITERATIONS, ranks=ranks)
+        view = e2e.upload(stream)
+        bw.pagerank(ctx, view, variant, ITERATIONS, ranks=ranks)
         out_host.copy_(ranks, non_blocking=True)
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t)
-    e2e_s = max(np.mean(e2e_times), 1e-9)
+    e2e_s = float(np.mean(e2e_times))
     if ws > 1:
         t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = ws * m * ITERATIONS / e2e_s / 1e9
+    h2d = e2e.h2d_bytes
+    del g, e2e
+    torch.cuda.empty_cache()
 
-    # ---- CPU baseline (rank 0, N=1): bounded sample on all host cores ----
+    extras = {}
+    if not args.no_bfs:
+        extras["learned_switch"] = bfs_learned_vs_fixed(ctx, dev)
+    if not args.no_batched:
+        extras["batched"] = batched(ctx, dev, args.batch_graphs)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(host, n, m, iterations=args.cpu_iterations)
@@ -213,20 +364,20 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"pagerank R-MAT scale {SCALE} edge factor {EDGE_FACTOR} seed {SEED}, "
-                               f"{ITERATIONS} iterations, variant {variant}",
+                               f"{ITERATIONS} iterations, fastest variant ({variant})",
                    "vertices": n, "edges": m, "iterations": ITERATIONS, "variant": variant,
                    "l2": "inputs larger than L2 (graph %.0f MB > 129 MB)" % ((4 * (n + 1) + 4 * m) / 1e6),
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"independent replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "k_pr_pull_segmented", "kernel_ms": round(kernel_ms, 5),
-                     "algorithmic_bytes": alg_bytes, "peak_source": peak_kind},
-        "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS",
-                "h2d_bytes_per_step": int(rv.numel() * 4 + re.numel() * 4),
+                     "kernel": DOMINANT.get(variant, "k_pr_edge"), "kernel_ms": round(kernel_ms, 5),
+                     "algorithmic_bytes": ab, "peak_source": peak_kind},
+        "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n * 4)},
         "gpu_launches": pagerank_launches(variant, ITERATIONS) * args.steps,
         "clocks": clocks.summary(),
     }
+    result.update(extras)
     if cpu is not None:
         result["cpu_baseline"] = cpu
     if rank == 0:
@@ -235,55 +386,68 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(host, n, m, iterations):
-    import oracle
-    threads = os.cpu_count() or 1
-    deg = np.diff(host["fwd_vertices"].astype(np.int64)).astype(np.uint32)
-    t = time.perf_counter()
-    oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], iterations, deg=deg, threads=threads)
-    dt = time.perf_counter() - t
-    return {"value": round(m * iterations / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": f"{iterations} of {ITERATIONS} iterations of the same R-MAT-{SCALE} PageRank "
-                      f"(vertex-pull + consolidateRank restated, OpenMP), {dt:.2f} s"}
-
-
 def run_reference(args):
     """CPU restatement of the reference path, timed on the host cores."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    import belewitte_gb300 as bw
     import torch
+
+    import belewitte_gb300 as bw
+    import oracle
     g = bw.DeviceGraph.generate("rmat", scale=SCALE, edge_factor=EDGE_FACTOR, seed=SEED,
                                 reps=bw.REP_FWD_CSR | bw.REP_REV_CSR)
     host = g.to_host_arrays()
     n, m = g.vertex_count, g.edge_count
     del g
     torch.cuda.empty_cache()
-    import oracle
     threads = os.cpu_count() or 1
     deg = np.diff(host["fwd_vertices"].astype(np.int64)).astype(np.uint32)
-    per_step_iters = args.cpu_iterations
+    per_step = args.cpu_iterations
     for _ in range(args.warmup):
         oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], 1, deg=deg, threads=threads)
     t = time.perf_counter()
     for _ in range(args.steps):
-        oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], per_step_iters, deg=deg,
-                                 threads=threads)
+        oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], per_step, deg=deg, threads=threads)
     dt = time.perf_counter() - t
-    value = m * per_step_iters * args.steps / dt / 1e9
-    sample = (f"{per_step_iters} PageRank iterations per step on the R-MAT-{SCALE} graph "
-              f"(vertex-pull + consolidateRank restated, OpenMP)")
+    value = m * per_step * args.steps / dt / 1e9
+    sample = (f"{per_step} PageRank iterations per step on the R-MAT-{SCALE} graph "
+              f"(vertex-pull + consolidateRank restated, OpenMP; the reference has no CPU PageRank)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"pagerank R-MAT scale {SCALE} edge factor {EDGE_FACTOR} seed {SEED}, "
                                f"{ITERATIONS} iterations", "vertices": n, "edges": m},
-        "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def run_case(spec: str):
+    """Small, self-contained runs for profiler captures."""
+    import torch
+
+    import belewitte_gb300 as bw
+    algo, variant, graph = spec.split(":")
+    ctx = bw.Context(0)
+    if graph == "er":
+        g = bw.DeviceGraph.generate("er", n=4194304, m=67108864, seed=23, reps=63)
+    elif graph == "rmat24s":
+        g = bw.DeviceGraph.generate("rmat", scale=24, edge_factor=16, seed=24, symmetrise=True, reps=63)
+    elif graph == "grid":
+        g = bw.DeviceGraph.generate("grid", h=4096, w=4096, reps=63)
+    else:
+        g = bw.DeviceGraph.generate("rmat", scale=22, edge_factor=16, seed=22, reps=63)
+    if algo == "pagerank":
+        bw.pagerank(ctx, g, variant, 3)
+    elif algo == "learned":
+        from belewitte_gb300 import learn
+        learn.run_learned(ctx, g, learn.load_predictor(), 0, loop="graph", stats=False)
+    else:
+        bw.bfs(ctx, g, variant, int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item()), loop="graph")
+    torch.cuda.synchronize()
+    print("case done", spec)
 
 
 def main():
@@ -292,12 +456,18 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--variant", default=HEADLINE_VARIANT)
+    ap.add_argument("--variant", default="")
     ap.add_argument("--cpu-iterations", type=int, default=3)
+    ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-bfs", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--case", default="")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    if args.case:
+        run_case(args.case)
+        return
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
     else:

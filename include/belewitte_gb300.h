@@ -462,6 +462,44 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g,
                        uint32_t stats_capacity, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched persistent traversal                                              */
+/* ------------------------------------------------------------------------ */
+/*
+ * Many independent units in one persistent launch fed by a device work
+ * queue (an atomic cursor over a list ordered largest first); each CTA takes
+ * a unit and runs it to completion with CTA-level barriers between levels
+ * and iterations.  No counterpart in the reference, which runs one
+ * traversal per process (kernel-runner.cpp:222-256).
+ *
+ * BW_BATCH_GRAPHS: `g` is one concatenated CSR (forward + reverse, global
+ *   vertex ids) of graph_count graphs; graph i owns vertices
+ *   [graph_offsets[i], graph_offsets[i+1]).  Unit i = graph i: BFS from
+ *   roots[i] (a global id), depths into levels[global id], then
+ *   pr_iterations PageRank iterations of graph i alone (its own N in the
+ *   base term, vertex-pull order: bit-identical to bw_pagerank_run on that
+ *   graph) into ranks[global id].
+ * BW_BATCH_SOURCES: graph_count = 1; unit i = BFS from roots[i];
+ *   depths into levels[i * vertex_count + v].
+ * graph_offsets, roots and `order` (unit ids, largest first; NULL = 0..n-1)
+ * are device arrays.
+ */
+enum bw_batch_mode { BW_BATCH_GRAPHS = 0, BW_BATCH_SOURCES = 1 };
+
+typedef struct bw_batch_result {
+    uint64_t units;             /* units run */
+    uint64_t traversed_edges;   /* BFS: sum over units of out-edges of reached vertices */
+    double device_ms;
+} bw_batch_result;
+
+int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode,
+                 const uint32_t *graph_offsets, uint32_t graph_count,
+                 const uint32_t *roots, const uint32_t *order,
+                 uint32_t unit_count, uint32_t max_unit_vertices,
+                 uint32_t pr_iterations, int32_t *levels, float *ranks,
+                 const bw_launch_config *cfg, bw_batch_result *result,
+                 void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Allocation-free BFS                                                       */
 /* ------------------------------------------------------------------------ */
 /*
