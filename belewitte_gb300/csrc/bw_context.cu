@@ -201,6 +201,7 @@ int bw_context_create(int device, bw_context **out)
     ctx->max_threads_per_block = prop.maxThreadsPerBlock;
     ctx->max_smem_per_block = prop.sharedMemPerBlock;
     ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
+    ctx->max_smem_per_sm = prop.sharedMemPerMultiprocessor;
     if (cudaEventCreate(&ctx->ev_start) != cudaSuccess ||
         cudaEventCreate(&ctx->ev_stop) != cudaSuccess) {
         bw_context_destroy(ctx);

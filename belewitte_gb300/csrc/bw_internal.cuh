@@ -99,6 +99,7 @@ struct bw_context {
     int max_threads_per_block = 1024;
     size_t max_smem_per_block = 0;
     size_t max_smem_optin = 0;
+    size_t max_smem_per_sm = 0;
 
     // BFS scratch
     bw::BfsCtl *bfs_ctl = nullptr;        // device

@@ -21,8 +21,10 @@
 #include <algorithm>
 #include <cstring>
 #include <cooperative_groups.h>
+#include <cub/cub.cuh>
 
 #include "bw_consolidate.h"
+#include "bw_seqsum.h"
 #include "bw_internal.cuh"
 
 namespace bw {
@@ -72,6 +74,17 @@ struct PrArgs {
     const uint4 *work;         // pull-segmented work items
     uint32_t work_count;
     uint32_t *long_count;      // arrival counters of split rows
+    float *vals;               // exact long rows: gathered terms, indexed by edge
+    // Hub-first source order (work-list kernels): the gathered array is
+    // stored at slot[v] and gat_e holds the reverse-CSR sources translated to
+    // slots (slot == nullptr: identity, gat_e == rev_e).  The nodiv family
+    // keeps its ranks in vertex order and writes the gathered copy to
+    // gat_out[slot[v]] (read as gat_in next iteration).
+    const uint32_t *gat_e;
+    const uint32_t *slot;
+    uint32_t hub_count;        // work-list kernels: gathered entries cached in shared memory
+    const float *gat_in;
+    float *gat_out;
     double base_div;           // (1.0 - 0.85f) / N, computed once on the host
 };
 
@@ -124,18 +137,58 @@ __global__ void __launch_bounds__(256) k_count_ids(const uint32_t *__restrict__ 
     }
 }
 
-// Initial ranks 1/N (pagerank/pagerank.cpp:88) and contributions.
-__global__ void k_pr_init(PrArgs a, float *pr, float *contrib, int rowlen)
+// Initial ranks 1/N (pagerank/pagerank.cpp:88) and contributions (stored at
+// the vertex's slot when sources are relabelled; `gat` is the nodiv family's
+// relabelled copy of the ranks).
+__global__ void k_pr_init(PrArgs a, float *pr, float *contrib, float *gat, int rowlen)
 {
     const float init = __fdiv_rn(1.0f, static_cast<float>(a.n));
     for (uint64_t v = gtid(); v < a.n; v += gthreads()) {
         pr[v] = init;
         if (a.acc) a.acc[v] = 0.0f;
+        const uint64_t at = a.slot ? a.slot[v] : v;
         if (contrib) {
             const uint32_t d = rowlen ? a.fwd_v[v + 1] - a.fwd_v[v] : a.deg[v];
-            contrib[v] = d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f;
+            contrib[at] = d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f;
+        }
+        if (gat) gat[at] = init;
+    }
+}
+
+// ----------------------- hub-first source order -----------------------------
+// Gathers dominate the pull kernels; a source is gathered once per out-edge.
+// Storing the gathered array in decreasing out-degree order packs the hubs
+// of skewed graphs into few cache lines, which then stay in L1.  Rows keep
+// their order and their sources' order, so every sum is unchanged.
+__global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint64_t n, uint32_t *__restrict__ keys,
+                               uint32_t *__restrict__ ids)
+{
+    for (uint64_t v = gtid(); v < n; v += gthreads()) {
+        const uint32_t d = deg[v];
+        keys[v] = d ? static_cast<uint32_t>(__clz(d)) : 32u;   // larger degree, smaller key
+        ids[v] = static_cast<uint32_t>(v);
+    }
+}
+
+__global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, uint32_t *__restrict__ slot)
+{
+    for (uint64_t i = gtid(); i < n; i += gthreads()) slot[order[i]] = static_cast<uint32_t>(i);
+}
+
+__global__ void __launch_bounds__(256) k_relabel_edges(const uint32_t *__restrict__ src, uint64_t m,
+                                                       const uint32_t *__restrict__ slot, uint32_t *__restrict__ out)
+{
+    const uint64_t quads = m / 4;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *o4 = reinterpret_cast<uint4 *>(out);
+    const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    if (aligned) {
+        for (uint64_t q = gtid(); q < quads; q += gthreads()) {
+            const uint4 x = __ldcs(s4 + q);
+            __stcs(o4 + q, make_uint4(__ldg(slot + x.x), __ldg(slot + x.y), __ldg(slot + x.z), __ldg(slot + x.w)));
         }
     }
+    for (uint64_t i = (aligned ? quads * 4 : 0) + gtid(); i < m; i += gthreads()) out[i] = __ldg(slot + src[i]);
 }
 
 // consolidateRank (div) for the atomic variants; also produces the next
@@ -147,11 +200,12 @@ __global__ void __launch_bounds__(256) k_consolidate_div(PrArgs a, int rowlen)
     for (uint64_t base = (gtid() >> 5) * 32; base < n; base += (gthreads() >> 5) * 32) {
         const uint64_t v = base + (threadIdx.x & 31);
         if (v < n) {
-            const float nr = consolidate_div(a.acc[v], a.base_div);
-            dsum += fabsf(nr - a.pr_out[v]);
+            const float acc = a.acc[v], prev = a.pr_out[v];
+            const uint32_t d = rowlen ? a.fwd_v[v + 1] - a.fwd_v[v] : a.deg[v];
+            const float nr = consolidate_div(acc, a.base_div);
+            dsum += fabsf(nr - prev);
             a.pr_out[v] = nr;
             a.acc[v] = 0.0f;
-            const uint32_t d = rowlen ? a.fwd_v[v + 1] - a.fwd_v[v] : a.deg[v];
             a.contrib_out[v] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
         }
     }
@@ -235,6 +289,34 @@ __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
     }
 }
 
+// Consolidate vertex v from its in-sum (div: consolidateRank plus the next
+// contribution; nodiv: consolidateRankNoDiv).  Returns |pr_new - pr_old|.
+template<bool NODIV>
+__device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, float sum, float base_nd)
+{
+    if constexpr (!NODIV) {
+        // both loads before the first store: the arrays are not restrict,
+        // so a load after a store would wait for it
+        const float prev = a.pr_out[v];
+        const uint32_t dg = a.deg[v];
+        const uint64_t at = a.slot ? a.slot[v] : v;
+        const float nr = consolidate_div(sum, a.base_div);
+        a.pr_out[v] = nr;
+        a.contrib_out[at] = dg ? __fdiv_rn(nr, static_cast<float>(dg)) : 0.0f;
+        return fabsf(nr - prev);
+    } else {
+        const float prev = a.pr_in[v];
+        const uint32_t dg = a.deg[v];
+        const uint32_t at = a.gat_out ? a.slot[v] : 0u;
+        float nr = __fmaf_rn(DAMPING, sum, base_nd);
+        const float d = fabsf(nr - prev);
+        if (dg != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(dg));
+        a.pr_out[v] = nr;
+        if (a.gat_out) a.gat_out[at] = nr;
+        return d;
+    }
+}
+
 // ----------------------------- pull variants ------------------------------
 // vertex-pull-warp / -nodiv (pagerank/vertex_pull_warp.cu:4-49,
 // vertex_pull_warp_nodiv.cu:4-47): a virtual warp of W lanes per vertex
@@ -265,19 +347,7 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
             for (uint32_t o = W >> 1; o > 0; o >>= 1) part += __shfl_xor_sync(mask, part, o, W);
             if (lane == 0) {
                 const uint64_t x = v0 + v;
-                if constexpr (!NODIV) {
-                    const float nr = consolidate_div(part, a.base_div);
-                    dsum += fabsf(nr - a.pr_out[x]);
-                    a.pr_out[x] = nr;
-                    const uint32_t d = a.deg[x];
-                    a.contrib_out[x] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
-                } else {
-                    float nr = __fmaf_rn(DAMPING, part, base_nd);
-                    dsum += fabsf(nr - a.pr_in[x]);
-                    const uint32_t d = a.deg[x];
-                    if (d != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(d));
-                    a.pr_out[x] = nr;
-                }
+                dsum += finish_vertex<NODIV>(a, x, part, base_nd);
             }
         }
         __syncwarp(mask);
@@ -298,40 +368,56 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
 // row's values one after the other in row order -- the reference's
 // sequential summation (pagerank/vertex_pull.cu:23-27), so these rows are
 // bit-identical to it.
-// Long rows, EXACT (vertex-pull, vertex-pull-nodiv): one warp streams the
-// row in 1024-edge chunks (parallel gathers into shared memory) and lane 0
-// keeps the single sequential sum -- bit-identical, bounded by the add
-// chain of the longest row.
-// Long rows, split (pull-segmented): 1024-edge pieces summed by any warp
-// (lane partials + shuffle tree), combined in acc[] by float atomics; the
-// last piece to arrive (arrival counter) consolidates the row.
+// Long rows (more than SEG_LONG edges) are cut into SEG_EDGES-edge pieces
+// that any warp takes; the work list puts every piece before the short-row
+// items so that long rows finish early.  The last piece of a row to arrive
+// (arrival counter) completes it:
+//   EXACT (vertex-pull, vertex-pull-nodiv): pieces store their gathered
+//   terms in vals[] (edge order); the last one evaluates the row's
+//   sequential sum with the whole warp (warp_sequential_sum, bit-identical
+//   to the reference's loop) and consolidates the vertex.
+//   split (pull-segmented): pieces add lane partials (shuffle tree) into
+//   acc[] with float atomics; the last one consolidates the row.
 constexpr uint32_t SEG_EDGES = 512;
 constexpr uint32_t SEG_LONG = 256;
 constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
-constexpr uint32_t LONG_FLAG = 0x40000000u;    // whole long row
+constexpr uint32_t LONG_FLAG = 0x40000000u;    // exact piece of a long row
 constexpr uint32_t ROW_MASK = 0x3fffffffu;
-constexpr int PULL_WARPS = 8;                  // warps per block
+// Two block shapes: WIDE, one block of 32 warps per SM, and NARROW, blocks
+// of 8 warps, several per SM (more warps in flight, fewer registers).
+// Shared memory holds each warp's gather buffer and, after it, a cache of
+// the first hub_count entries of the gathered array: with sources in
+// hub-first order those are the most gathered values of the graph, read
+// from shared memory instead of L2.  Every block holds its own copy, and
+// what shared memory takes is lost to L1, which bounds the misses in flight.
+constexpr int PULL_WIDE = 1024, PULL_NARROW = 256;
+constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (SEG_EDGES + 33) * sizeof(float); }
+constexpr int pull_min_blocks(int block, bool exact) { return block == PULL_WIDE ? 1 : (exact ? 4 : 5); }
+// default hub-cache entries per block
+constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
 constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
-__global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, int split, uint32_t *__restrict__ counts)
+__global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ counts)
 {
-    // one thread per 32-row window: number of work items it will emit
+    // one thread per 32-row window: the long-row pieces it will emit
+    // (counts[w]) and its short-row items (counts[windows + w])
     const uint64_t windows = (n + 31) / 32;
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
         const uint64_t r0 = w * 32, r1 = min(n, r0 + 32);
-        uint32_t items = 0, acc_edges = 0, acc_rows = 0;
+        uint32_t pieces = 0, items = 0, acc_edges = 0, acc_rows = 0;
         for (uint64_t r = r0; r < r1; r++) {
             const uint32_t d = off[r + 1] - off[r];
             if (d > SEG_LONG) {
                 if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
-                items += split ? (d + SEG_EDGES - 1) / SEG_EDGES : 1;
+                pieces += (d + SEG_EDGES - 1) / SEG_EDGES;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) { items++; acc_rows = 0; acc_edges = 0; }
             acc_rows++; acc_edges += d;
         }
         if (acc_rows) items++;
-        counts[w] = items;
+        counts[w] = pieces;
+        counts[windows + w] = items;
     }
 }
 
@@ -340,9 +426,10 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n, int spl
                            uint32_t *__restrict__ long_count)
 {
     const uint64_t windows = (n + 31) / 32;
+    const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
         const uint64_t r0 = w * 32, r1 = min(n, r0 + 32);
-        uint32_t out = first[w];
+        uint32_t piece_out = first[w], out = first[windows + w];
         uint64_t start_row = r0;
         uint32_t acc_edges = 0, acc_rows = 0;
         for (uint64_t r = r0; r < r1; r++) {
@@ -352,14 +439,10 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n, int spl
                     work[out++] = make_uint4(uint32_t(start_row), uint32_t(r), off[start_row], off[r]);
                     acc_rows = 0; acc_edges = 0;
                 }
-                if (split) {
-                    for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
-                        work[out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | PIECE_FLAG, p,
-                                                 min(p + SEG_EDGES, off[r + 1]));
-                    long_count[r] = 0;
-                } else {
-                    work[out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | LONG_FLAG, off[r], off[r + 1]);
-                }
+                for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
+                    work[piece_out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | flag, p,
+                                                   min(p + SEG_EDGES, off[r + 1]));
+                long_count[r] = 0;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) {
@@ -373,30 +456,17 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n, int spl
     }
 }
 
-// Consolidate vertex v from its in-sum (div: consolidateRank plus the next
-// contribution; nodiv: consolidateRankNoDiv).  Returns |pr_new - pr_old|.
-template<bool NODIV>
-__device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, float sum, float base_nd)
+
+// One gathered value: from the shared-memory hub cache when the source is
+// among the first `hubs` entries, else from global memory.
+__device__ __forceinline__ float gather1(const float *__restrict__ src, const float *hub, uint32_t hubs, uint32_t i)
 {
-    if constexpr (!NODIV) {
-        const float nr = consolidate_div(sum, a.base_div);
-        const float d = fabsf(nr - a.pr_out[v]);
-        a.pr_out[v] = nr;
-        const uint32_t dg = a.deg[v];
-        a.contrib_out[v] = dg ? __fdiv_rn(nr, static_cast<float>(dg)) : 0.0f;
-        return d;
-    } else {
-        float nr = __fmaf_rn(DAMPING, sum, base_nd);
-        const float d = fabsf(nr - a.pr_in[v]);
-        const uint32_t dg = a.deg[v];
-        if (dg != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(dg));
-        a.pr_out[v] = nr;
-        return d;
-    }
+    return i < hubs ? hub[i] : __ldg(src + i);
 }
 
 // Gather src[rev_e[e0 + k]] for k in [0, len) (len <= SEG_EDGES) into buf.
 __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, const float *__restrict__ src,
+                                            const float *hub, uint32_t hubs,
                                             uint32_t e0, uint32_t len, float *buf, unsigned lane)
 {
     for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
@@ -410,7 +480,7 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
 #pragma unroll
         for (int u = 0; u < GATHER_UNROLL; u++) {
             const uint32_t k = base + u * 32 + lane;
-            v[u] = k < len ? __ldg(src + idx[u]) : 0.0f;
+            v[u] = k < len ? gather1(src, hub, hubs, idx[u]) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < GATHER_UNROLL; u++) {
@@ -420,33 +490,168 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
     }
 }
 
-template<bool NODIV, bool EXACT_LONG>
-__global__ void __launch_bounds__(PULL_WARPS * 32, 5) k_pr_pull_items(PrArgs a)
+// The sequential sum s = fl(s + vals[i]), i = 0..n-1, starting from +0 --
+// bit-identical to one thread's loop -- evaluated window by window (256
+// terms, staged in shared memory).  The first SERIAL_TERMS terms are added
+// by lane 0 in order: there the sum still doubles every few terms, so nearly
+// every window would cross a binade.  Later windows use the binade maps of
+// bw_seqsum.h: 8 consecutive terms per lane, a scan of the lanes' maps, and
+// one float addition by the lane that holds the next binade crossing.
+// `stage` holds 264 floats of shared memory; `vals` was written in this
+// launch, so it is read through L2.  Every lane returns the sum.
+constexpr uint32_t SERIAL_TERMS = 1024;
+
+__device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t n, float *stage, unsigned lane)
 {
-    __shared__ __align__(16) float s_val[PULL_WARPS][SEG_EDGES];
-    __shared__ uint32_t s_end[PULL_WARPS][33];
+    using namespace bwseq;
+    constexpr uint32_t L = 8, WIN = 32 * L;
+    uint32_t sb = 0;                       // bits of the running sum (warp-uniform)
+    bool ok = true;
+    float pre[L];
+#pragma unroll
+    for (uint32_t u = 0; u < L; u++) pre[u] = u * 32 + lane < n ? __ldcg(vals + u * 32 + lane) : 0.0f;
+    for (uint32_t w = 0; w < n && ok; w += WIN) {
+        // window [w, w + WIN): coalesced loads, staged so that lane l reads
+        // terms 8l..8l+7 (element k at k + k / 32: no bank conflicts)
+#pragma unroll
+        for (uint32_t u = 0; u < L; u++) stage[u * 33 + lane] = pre[u];
+        __syncwarp();
+        uint32_t x[L];
+#pragma unroll
+        for (uint32_t u = 0; u < L; u++) {
+            const uint32_t k = lane * L + u;
+            x[u] = __float_as_uint(stage[k + (k >> 5)]);
+        }
+        __syncwarp();
+        const uint32_t nw = w + WIN;
+#pragma unroll
+        for (uint32_t u = 0; u < L; u++)
+            pre[u] = nw + u * 32 + lane < n ? __ldcg(vals + nw + u * 32 + lane) : 0.0f;
+        const uint32_t lim = min(WIN, n - w), first = lane * L;
+        if (w < SERIAL_TERMS) {            // early terms: lane 0 adds them in order
+            uint32_t bits = 0;
+            if (lane == 0) {
+                float acc = __uint_as_float(sb);
+                for (uint32_t i = 0; i < lim; i++) acc = __fadd_rn(acc, stage[i + (i >> 5)]);
+                bits = __float_as_uint(acc);
+            }
+            sb = __shfl_sync(FULL_MASK, bits, 0);
+            __syncwarp();
+            continue;
+        }
+        uint32_t pos = 0;                  // first term of the window not yet added
+        for (uint32_t guard = 0; pos < lim; guard++) {
+            if (guard > WIN + 1) { ok = false; break; }
+            if (sb == 0) {
+                // the sum is still +0: it becomes the first nonzero term
+                uint32_t hit = L, hv = 0;
+#pragma unroll
+                for (uint32_t u = 0; u < L; u++)
+                    if (hit == L && first + u >= pos && first + u < lim && (x[u] & 0x7fffffffu)) { hit = u; hv = x[u]; }
+                const unsigned any = __ballot_sync(FULL_MASK, hit < L);
+                if (!any) break;
+                const unsigned f = __ffs(any) - 1;
+                sb = __shfl_sync(FULL_MASK, hv, f);
+                pos = f * L + __shfl_sync(FULL_MASK, hit, f) + 1;
+                if (!in_domain(sb)) { ok = false; break; }
+                continue;
+            }
+            if (!in_domain(sb)) { ok = false; break; }
+            const uint32_t K = exponent_of(sb), A = significand_of(sb);
+            Map m = identity();
+            bool bad = false;
+#pragma unroll
+            for (uint32_t u = 0; u < L; u++) {
+                if (first + u >= pos && first + u < lim) {
+                    Map t;
+                    bad |= !step(x[u], K, t);
+                    m = compose(m, t);
+                }
+            }
+            if (__any_sync(FULL_MASK, bad)) { ok = false; break; }
+            Map incl = m;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const Map y{__shfl_up_sync(FULL_MASK, incl.e, o), __shfl_up_sync(FULL_MASK, incl.o, o)};
+                if (lane >= static_cast<unsigned>(o)) incl = compose(y, incl);
+            }
+            Map excl{__shfl_up_sync(FULL_MASK, incl.e, 1), __shfl_up_sync(FULL_MASK, incl.o, 1)};
+            if (lane == 0) excl = identity();
+            const uint32_t a0 = apply(excl, A), a1 = apply(m, a0);
+            const unsigned cross = __ballot_sync(FULL_MASK, a1 >= TOP);
+            if (!cross) {
+                sb = bits_of(K, __shfl_sync(FULL_MASK, a1, 31));
+                break;
+            }
+            // the first lane whose run leaves the binade finds the term
+            const unsigned f = __ffs(cross) - 1;
+            uint32_t nb = 0, np = 0;
+            if (lane == f) {
+                uint32_t acc = a0;
+#pragma unroll
+                for (uint32_t u = 0; u < L; u++) {
+                    if (np == 0 && first + u >= pos && first + u < lim) {
+                        Map t;
+                        step(x[u], K, t);
+                        const uint32_t b = apply(t, acc);
+                        if (b >= TOP) {
+                            nb = __float_as_uint(__fadd_rn(__uint_as_float(bits_of(K, acc)), __uint_as_float(x[u])));
+                            np = first + u + 1;
+                        } else {
+                            acc = b;
+                        }
+                    }
+                }
+            }
+            np = __shfl_sync(FULL_MASK, np, f);
+            sb = __shfl_sync(FULL_MASK, nb, f);
+            if (np <= pos || exponent_of(sb) == 0xffu) { ok = false; break; }
+            pos = np;
+        }
+    }
+    if (!ok) {                             // outside the domain: the plain loop
+        float s = 0.0f;
+        if (lane == 0)
+            for (uint32_t i = 0; i < n; i++) s = __fadd_rn(s, __ldcg(vals + i));
+        return __shfl_sync(FULL_MASK, s, 0);
+    }
+    return __uint_as_float(sb);
+}
+
+template<bool NODIV, bool EXACT_LONG, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_pr_pull_items(PrArgs a)
+{
+    constexpr int PULL_WARPS = BLOCK / 32;
+    extern __shared__ __align__(16) float smem_f[];
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
-    const float *src = NODIV ? a.pr_in : a.contrib_in;
+    const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
+    const uint32_t *ge = a.gat_e;
     const float base_nd = nodiv_base(a.n);
-    float *buf = s_val[wib];
+    float *buf = smem_f + wib * SEG_EDGES;
+    uint32_t *s_end = reinterpret_cast<uint32_t *>(smem_f + PULL_WARPS * SEG_EDGES) + wib * 33;
+    float *hub = smem_f + PULL_WARPS * (SEG_EDGES + 33);
+    const uint32_t hubs = a.hub_count;       // multiple of 4
+    for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
+        reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
+    __syncthreads();
     float dsum = 0.0f;
     for (uint64_t it = warp; it < a.work_count; it += warps) {
         const uint4 w = a.work[it];
         const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
-        if (w.y & PIECE_FLAG) {
+        if (!EXACT_LONG && (w.y & PIECE_FLAG)) {
             float part = 0.0f;
             for (uint32_t base = e0; base < e1; base += 32 * GATHER_UNROLL) {
                 uint32_t idx[GATHER_UNROLL];
 #pragma unroll
                 for (int u = 0; u < GATHER_UNROLL; u++) {
                     const uint32_t i = base + u * 32 + lane;
-                    idx[u] = i < e1 ? __ldcs(a.rev_e + i) : 0u;
+                    idx[u] = i < e1 ? __ldcs(ge + i) : 0u;
                 }
 #pragma unroll
                 for (int u = 0; u < GATHER_UNROLL; u++) {
                     const uint32_t i = base + u * 32 + lane;
-                    part += i < e1 ? __ldg(src + idx[u]) : 0.0f;
+                    part += i < e1 ? gather1(src, hub, hubs, idx[u]) : 0.0f;
                 }
             }
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
@@ -463,69 +668,59 @@ __global__ void __launch_bounds__(PULL_WARPS * 32, 5) k_pr_pull_items(PrArgs a)
             }
             continue;
         }
-        if (w.y & LONG_FLAG) {
-            // Lane 0 keeps the sequential sum of chunk c while lanes 1..31
-            // gather chunk c + 1 into the other half of the warp's buffer.
-            float *half[2] = {buf, buf + SEG_EDGES / 2};
-            constexpr uint32_t CH = SEG_EDGES / 2;
-            const uint32_t nch = (e1 - e0 + CH - 1) / CH;
-            auto gather31 = [&](uint32_t c, float *dst) {
-                const uint32_t b0 = e0 + c * CH, cnt = min(CH, e1 - b0);
-                if (lane == 0) return;
-                constexpr int U = (CH + 30) / 31;
-                uint32_t idx[U];
+        if (EXACT_LONG && (w.y & LONG_FLAG)) {
+            // exact piece: store the gathered terms, the last piece sums the row
+            const uint32_t len = e1 - e0;
+            for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
+                uint32_t idx[GATHER_UNROLL];
 #pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const uint32_t k = (lane - 1) + 31 * u;
-                    idx[u] = k < cnt ? __ldcs(a.rev_e + b0 + k) : 0u;
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t k = base + u * 32 + lane;
+                    idx[u] = k < len ? __ldcs(ge + e0 + k) : 0u;
                 }
 #pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const uint32_t k = (lane - 1) + 31 * u;
-                    if (k < cnt) dst[k] = __ldg(src + idx[u]);
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t k = base + u * 32 + lane;
+                    if (k < len) __stcg(a.vals + e0 + k, gather1(src, hub, hubs, idx[u]));
                 }
-            };
-            gather31(0, half[0]);
-            __syncwarp();
-            float sum = 0.0f;
-            for (uint32_t c = 0; c < nch; c++) {
-                if (c + 1 < nch) gather31(c + 1, half[(c + 1) & 1]);
-                if (lane == 0) {
-                    const float *q = half[c & 1];
-                    const uint32_t cnt = min(CH, e1 - (e0 + c * CH));
-                    uint32_t i = 0;
-                    for (; i + 4 <= cnt; i += 4) {
-                        const float4 v = *reinterpret_cast<const float4 *>(q + i);
-                        sum = __fadd_rn(sum, v.x); sum = __fadd_rn(sum, v.y);
-                        sum = __fadd_rn(sum, v.z); sum = __fadd_rn(sum, v.w);
-                    }
-                    for (; i < cnt; i++) sum = __fadd_rn(sum, q[i]);
-                }
-                __syncwarp();
             }
-            if (lane == 0) dsum += finish_vertex<NODIV>(a, r0, sum, base_nd);
+            __threadfence();
+            __syncwarp();
+            const uint32_t row_begin = a.rev_v[r0], row_len = a.rev_v[r0 + 1] - row_begin;
+            uint32_t last = 0;
+            if (lane == 0) {
+                const uint32_t pieces = (row_len + SEG_EDGES - 1) / SEG_EDGES;
+                last = atomicAdd(&a.long_count[r0], 1u) + 1 == pieces;
+            }
+            if (__shfl_sync(FULL_MASK, last, 0)) {
+                __threadfence();
+                const float total = warp_sequential_sum(a.vals + row_begin, row_len, buf, lane);
+                if (lane == 0) {
+                    a.long_count[r0] = 0;
+                    dsum += finish_vertex<NODIV>(a, r0, total, base_nd);
+                }
+            }
             continue;
         }
         // up to 32 short rows
         const uint32_t rows = r1 - r0, len = e1 - e0;
-        if (lane < rows) s_end[wib][lane] = a.rev_v[r0 + lane + 1] - e0;
-        gather_into(a.rev_e, src, e0, len, buf, lane);
+        if (lane < rows) s_end[lane] = a.rev_v[r0 + lane + 1] - e0;
+        gather_into(ge, src, hub, hubs, e0, len, buf, lane);
         __syncwarp();
         if (lane < rows) {
-            const uint32_t b = lane ? s_end[wib][lane - 1] : 0u, e = s_end[wib][lane];
+            const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
             float sum = 0.0f;
             for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
             dsum += finish_vertex<NODIV>(a, r0 + lane, sum, base_nd);
         }
         __syncwarp();
     }
-    (void) EXACT_LONG;
     add_diff(a.diff, dsum);
 }
 
 __global__ void k_exclusive_scan_small(uint32_t *data, uint64_t count, uint32_t *total)
 {
-    // single block scan used for the work-item layout (count = N/32)
+    // single block scan used for the work-item layout (count = 2 x N/32)
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -588,6 +783,7 @@ struct PrRun {
     uint32_t work_count = 0;
     uint32_t *long_count = nullptr;
     uint32_t *win_counts = nullptr;
+    float *vals = nullptr;             // exact long rows: gathered terms (edge-indexed)
 };
 
 struct Geometry { unsigned block, grid; size_t smem; };
@@ -595,8 +791,15 @@ struct Geometry { unsigned block, grid; size_t smem; };
 Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cfg)
 {
     Geometry g{256, static_cast<unsigned>(ctx->sm_count) * 8, 0};
-    if (variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV || variant == PR_PULL_SEGMENTED)
-        g.grid = static_cast<unsigned>(ctx->sm_count) * 5;   // one resident wave (register bound)
+    if (variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV) {
+        // block_size picks the shape (default NARROW); one resident wave
+        const bool exact = variant != PR_PULL_SEGMENTED;
+        g.block = (cfg && cfg->block_size == PULL_WIDE) ? PULL_WIDE : PULL_NARROW;
+        g.grid = static_cast<unsigned>(ctx->sm_count) * pull_min_blocks(static_cast<int>(g.block), exact);
+        if (cfg && cfg->grid_size) g.grid = cfg->grid_size;
+        g.smem = pull_fixed_smem(static_cast<int>(g.block));  // + the hub cache (run_pagerank)
+        return g;
+    }
     const uint32_t W = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
     const uint32_t C = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
     if (cfg && cfg->block_size) g.block = cfg->block_size;
@@ -610,16 +813,22 @@ Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cf
 int validate_cfg(const bw_context *ctx, int variant, const bw_launch_config *cfg)
 {
     if (!cfg) return BW_OK;
+    const bool items = variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV;
+    if (items) {
+        // work-list kernels: block_size picks the shape, chunk_size the
+        // hub-cache entries per block (a multiple of 4)
+        if (cfg->block_size && cfg->block_size != PULL_WIDE && cfg->block_size != PULL_NARROW)
+            return BW_ERR_INVALID_ARGUMENT;
+        if (cfg->chunk_size % 4) return BW_ERR_INVALID_ARGUMENT;
+        return BW_OK;
+    }
     if (cfg->block_size && (cfg->block_size % 32 || cfg->block_size > 256)) {
-        // every PageRank kernel is built for at most 256 threads, the warp
-        // variants for 512
+        // every other PageRank kernel is built for at most 256 threads, the
+        // warp variants for 512
         const bool warp = variant == PR_VERTEX_PUSH_WARP || variant == PR_VERTEX_PULL_WARP ||
                           variant == PR_VERTEX_PULL_WARP_NODIV;
         if (cfg->block_size % 32 || cfg->block_size > (warp ? 512u : 256u)) return BW_ERR_INVALID_ARGUMENT;
     }
-    if ((variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV) &&
-        cfg->block_size && cfg->block_size != PULL_WARPS * 32)
-        return BW_ERR_INVALID_ARGUMENT;
     const uint32_t W = cfg->warp_size ? cfg->warp_size : 32;
     const uint32_t C = cfg->chunk_size ? cfg->chunk_size : 32;
     // ImplementationTemplate.hpp:463-471: power-of-two W <= 32, C % W == 0.
@@ -658,17 +867,21 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     // Row groups <= N; pieces <= M / SEG_EDGES + (rows longer than
     // SEG_LONG) <= M / SEG_EDGES + M / SEG_LONG.
     const uint64_t cap = windows + n + g->edge_count / SEG_EDGES + g->edge_count / SEG_LONG + 16;
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.win_counts), (windows + 1) * sizeof(uint32_t), s));
+    // counts: [pieces of window 0..W-1 | short items of window 0..W-1 | total]
+    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.win_counts), (2 * windows + 1) * sizeof(uint32_t), s));
     BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
     BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
-    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts);
-    k_exclusive_scan_small<<<1, 1024, 0, s>>>(run.win_counts, windows, run.win_counts + windows);
+    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, run.win_counts);
+    k_exclusive_scan_small<<<1, 1024, 0, s>>>(run.win_counts, 2 * windows, run.win_counts + 2 * windows);
     k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts, run.work, run.long_count);
     BW_CUDA(cudaGetLastError());
-    uint32_t count = 0;
-    BW_CUDA(cudaMemcpyAsync(&count, run.win_counts + windows, sizeof count, cudaMemcpyDeviceToHost, s));
+    uint32_t totals[2] = {0, 0};       // pieces (the exclusive prefix at W), all items
+    BW_CUDA(cudaMemcpyAsync(&totals[0], run.win_counts + windows, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    BW_CUDA(cudaMemcpyAsync(&totals[1], run.win_counts + 2 * windows, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     BW_CUDA(cudaStreamSynchronize(s));
-    run.work_count = count;
+    run.work_count = totals[1];
+    if (!split && totals[0])
+        BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.vals), g->edge_count * sizeof(float), s));
     return BW_OK;
 }
 
@@ -677,7 +890,8 @@ void free_run(PrRun &run, cudaStream_t s)
     if (run.work) cudaFreeAsync(run.work, s);
     if (run.long_count) cudaFreeAsync(run.long_count, s);
     if (run.win_counts) cudaFreeAsync(run.win_counts, s);
-    run.work = nullptr; run.long_count = nullptr; run.win_counts = nullptr;
+    if (run.vals) cudaFreeAsync(run.vals, s);
+    run.work = nullptr; run.long_count = nullptr; run.win_counts = nullptr; run.vals = nullptr;
 }
 
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
@@ -689,11 +903,20 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_REV_STRUCT_EDGE_LIST: k_pr_edge<3><<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_VERTEX_PUSH: k_pr_vertex_push<<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_VERTEX_PUSH_WARP: k_pr_vertex_push_warp<<<geo.grid, geo.block, geo.smem, s>>>(a); break;
-      case PR_VERTEX_PULL: k_pr_pull_items<false, true><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
-      case PR_VERTEX_PULL_NODIV: k_pr_pull_items<true, true><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
+      case PR_VERTEX_PULL:
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        break;
+      case PR_VERTEX_PULL_NODIV:
+        if (geo.block == PULL_WIDE) k_pr_pull_items<true, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<true, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        break;
       case PR_VERTEX_PULL_WARP: k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
       case PR_VERTEX_PULL_WARP_NODIV: k_pr_vertex_pull_warp<true><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
-      case PR_PULL_SEGMENTED: k_pr_pull_items<false, false><<<geo.grid, PULL_WARPS * 32, 0, s>>>(a); break;
+      case PR_PULL_SEGMENTED:
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        break;
       default: return BW_ERR_UNKNOWN_VARIANT;
     }
     if (!is_fused(variant)) {
@@ -702,6 +925,50 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
+
+// Scratch of the hub-first source order of one run.
+struct Relabel {
+    uint32_t *slot = nullptr;     // vertex -> position in the gathered array
+    uint32_t *gat_e = nullptr;    // reverse-CSR sources as positions
+    void *scratch = nullptr;
+};
+
+// Orders vertices by decreasing out-degree class (floor(log2(deg))), stable
+// in vertex order, and translates the reverse CSR's sources (one pass over
+// M).  Runs after the degrees, inside the timed region.
+int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, Relabel &r, cudaStream_t s)
+{
+    const uint64_t n = g->vertex_count, m = g->edge_count;
+    size_t temp = 0;
+    cub::DoubleBuffer<uint32_t> keys(nullptr, nullptr), ids(nullptr, nullptr);
+    BW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
+    const size_t words = 4 * n, temp_words = (temp + 3) / 4;
+    BW_CUDA(cudaMallocAsync(&r.scratch, (words + temp_words) * sizeof(uint32_t), s));
+    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
+    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
+    uint32_t *base = static_cast<uint32_t *>(r.scratch);
+    keys = cub::DoubleBuffer<uint32_t>(base, base + n);
+    ids = cub::DoubleBuffer<uint32_t>(base + 2 * n, base + 3 * n);
+    k_relabel_keys<<<ctx->sm_count * 4, 256, 0, s>>>(deg, n, keys.Current(), ids.Current());
+    BW_CUDA(cub::DeviceRadixSort::SortPairs(base + words, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
+    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.slot);
+    if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.slot, r.gat_e);
+    BW_CUDA(cudaGetLastError());
+    return BW_OK;
+}
+
+void free_relabel(Relabel &r, cudaStream_t s)
+{
+    if (r.scratch) cudaFreeAsync(r.scratch, s);
+    if (r.slot) cudaFreeAsync(r.slot, s);
+    if (r.gat_e) cudaFreeAsync(r.gat_e, s);
+    r = Relabel{};
+}
+
+// Hub-first order pays when the work-list kernels run several iterations
+// over a graph whose gathered array is larger than L1 many times over.
+constexpr uint64_t RELABEL_MIN_VERTICES = 1u << 16;
+constexpr uint32_t RELABEL_MIN_ITERATIONS = 3;
 
 // Runs a (possibly switching) schedule of variants of one semantics class.
 int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
@@ -715,9 +982,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         return BW_ERR_INVALID_ARGUMENT;
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
-    bool need_split = false, need_exact = false, any_rowlen = false, any_deg = false;
+    bool need_split = false, need_exact = false, any_rowlen = false, any_deg = false, all_items = true;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
+        all_items = all_items && (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV || v == PR_PULL_SEGMENTED);
         if (v < 0 || v >= PR_VARIANT_COUNT) return BW_ERR_UNKNOWN_VARIANT;
         if (is_nodiv(v) != nodiv) return BW_ERR_INVALID_ARGUMENT;
         BW_TRY(validate_cfg(ctx, v, cfg));
@@ -746,6 +1014,30 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.base_div = (1.0 - static_cast<double>(0.85f)) / static_cast<double>(n);
     a.deg = ctx->pr_deg;
     a.acc = ctx->pr_acc;
+    a.gat_e = g->rev_edges;
+    if (need_split || need_exact) {
+        // hub cache entries per block: chunk_size when given, else the
+        // default for the shape; never more than the block's share of
+        // shared memory allows
+        const int block = (cfg && cfg->block_size == PULL_WIDE) ? PULL_WIDE : PULL_NARROW;
+        const uint64_t per_sm = block == PULL_WIDE ? 1 : static_cast<uint64_t>(pull_min_blocks(block, need_exact));
+        const size_t fixed = pull_fixed_smem(block);
+        const size_t share = std::min<size_t>(ctx->max_smem_optin, ctx->max_smem_per_sm / per_sm);
+        const uint64_t room = share > fixed + 1024 ? (share - fixed - 1024) / sizeof(float) : 0;
+        const uint64_t want = (cfg && cfg->chunk_size) ? cfg->chunk_size
+                                                       : (block == PULL_WIDE ? PULL_WIDE_HUBS : PULL_NARROW_HUBS);
+        a.hub_count = static_cast<uint32_t>(std::min<uint64_t>(std::min<uint64_t>(n, room), want)) & ~3u;
+        const int bytes = static_cast<int>(fixed + a.hub_count * sizeof(float));
+        if (block == PULL_WIDE) {
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, false, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        } else {
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, false, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        }
+    }
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
     a.chunk_size = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
 
@@ -757,6 +1049,23 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         k_row_lengths<<<ctx->sm_count * 4, 256, 0, s>>>(g->fwd_vertices, n, ctx->pr_deg);
     }
     BW_CUDA(cudaMemsetAsync(ctx->pr_diffs, 0, (iterations + 1) * sizeof(float), s));
+    Relabel rl;
+    const bool relabel = all_items && n >= RELABEL_MIN_VERTICES && iterations >= RELABEL_MIN_ITERATIONS &&
+                         g->edge_count > 0;
+    if (relabel) {
+        const int rc = build_relabel(ctx, g, ctx->pr_deg, rl, s);
+        if (rc != BW_OK) {
+            free_relabel(rl, s);
+            free_run(split_run, s);
+            free_run(exact_run, s);
+            return rc;
+        }
+        a.slot = rl.slot;
+        a.gat_e = rl.gat_e;
+    }
+    // nodiv + relabelled sources: the gathered copy of the ranks, in slot order
+    float *gat[2] = {ctx->pr_buf[1], ctx->pr_acc};
+    const bool nodiv_gat = nodiv && relabel;
 
     // Buffers: div -> ranks in place, contributions double-buffered in
     // pr_buf[0/1]; nodiv -> ranks double-buffered between `ranks` and
@@ -769,7 +1078,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     }
     const int first_rowlen = uses_rowlen(schedule[0]) && !any_deg ? 1 : 0;
     k_pr_init<<<ctx->sm_count * 4, 256, 0, s>>>(a, nodiv ? nb[0] : ranks, nodiv ? nullptr : contrib[0],
-                                                 first_rowlen);
+                                                 nodiv_gat ? gat[0] : nullptr, first_rowlen);
     BW_CUDA(cudaGetLastError());
 
     for (uint32_t j = 1; j <= iterations; j++) {
@@ -780,6 +1089,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         if (nodiv) {
             a.pr_in = nb[(j - 1) & 1];
             a.pr_out = nb[j & 1];
+            if (nodiv_gat) {
+                a.gat_in = gat[(j - 1) & 1];
+                a.gat_out = gat[j & 1];
+            }
         } else {
             a.pr_out = ranks;
             if (is_fused(v)) {
@@ -795,6 +1108,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.work = items.work;
         a.work_count = items.work_count;
         a.long_count = items.long_count;
+        a.vals = items.vals;
         Geometry geo = geometry(ctx, v, cfg);
         BW_TRY(launch_iteration(ctx, v, a, geo, s));
         (void) loop_mode;
@@ -810,6 +1124,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     BW_CUDA(cudaStreamSynchronize(s));
     free_run(split_run, s);
     free_run(exact_run, s);
+    free_relabel(rl, s);
     if (time_iterations && iteration_ms) {
         for (uint32_t j = 0; j < iterations; j++)
             BW_CUDA(cudaEventElapsedTime(&iteration_ms[j], ctx->level_events[j], ctx->level_events[j + 1]));

@@ -16,6 +16,12 @@ def star(n):
     return bw.HostGraph.from_edges(n, np.zeros(n - 1, np.uint32), dst)
 
 
+def star_in(n):
+    """Every leaf points at vertex 0: one in-row of n - 1 equal terms."""
+    src = np.arange(1, n, dtype=np.uint32)
+    return bw.HostGraph.from_edges(n, src, np.zeros(n - 1, np.uint32))
+
+
 def catalog():
     """name -> (constructor, root) of the small parity graphs."""
     return {

@@ -65,6 +65,55 @@ def test_variant_parity(ctx, graphs, variant, iterations):
         assert _rel(got, r64) <= REL_F64, (name, gname)
 
 
+@pytest.fixture(scope="module")
+def long_graphs(ctx):
+    from tests.graphs import star_in
+    out = {}
+    for kind, h in (("star_in", star_in(200000)), ("rmat16", bw.HostGraph.rmat(16, 32, seed=3))):
+        out[kind] = (h, bw.DeviceGraph(h))
+    return out
+
+
+@pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
+@pytest.mark.parametrize("iterations", [1, 2, 30])
+def test_long_rows(ctx, long_graphs, variant, iterations):
+    """In-rows far longer than one work item: the exact variants evaluate
+    the sequential sum with the whole warp and must stay bit-identical,
+    including a 199,999-term row of equal terms (a round-half-even tie at
+    nearly every step) and R-MAT hubs.  On the equal-term row the
+    reference's own loop is far from FP64 (1.2e-3 after one iteration, 2e-5
+    after 30), so there the exact variants are held to the reference bits
+    only and pull-segmented, which reorders the sum, to FP64 only; on the
+    R-MAT graph every bound applies."""
+    for kind, (h, g) in long_graphs.items():
+        got = bw.pagerank(ctx, g, variant, iterations).ranks.cpu().numpy()
+        div, nodiv, d64, n64 = _oracles(h, iterations)
+        ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
+        if variant in BITEXACT:
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, kind)
+            if kind == "star_in":
+                continue
+        elif kind != "star_in":
+            assert _rel(got, ref) <= REL_REF, (variant, kind)
+        assert _rel(got, r64) <= REL_F64, (variant, kind)
+
+
+@pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
+@pytest.mark.parametrize("block,hubs", [(256, 0), (256, 4), (256, 2048), (1024, 0), (1024, 16384), (1024, 1 << 20)])
+def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs):
+    """Both block shapes of the work-list kernels, with and without the
+    shared-memory hub cache (sizes beyond the graph or the shared memory
+    are clamped): results do not depend on the shape."""
+    for name, (h, g) in list(long_graphs.items()) + [("rmat14", graphs["rmat14"]), ("chain", graphs["chain"])]:
+        got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs).ranks.cpu().numpy()
+        div, nodiv, _, _ = _oracles(h, 30)
+        ref = nodiv if "nodiv" in variant else div
+        if variant in BITEXACT:
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name, block, hubs)
+        elif name != "star_in":
+            assert _rel(got, ref) <= REL_REF, (variant, name, block, hubs)
+
+
 @pytest.mark.parametrize("variant", ["vertex-push-warp", "vertex-pull-warp", "vertex-pull-warp-nodiv"])
 @pytest.mark.parametrize("w,c", [(1, 1), (4, 8), (16, 64), (32, 32)])
 def test_warp_configs(ctx, graphs, variant, w, c):
