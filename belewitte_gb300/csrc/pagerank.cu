@@ -291,30 +291,48 @@ __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
 
 // Consolidate vertex v from its in-sum (div: consolidateRank plus the next
 // contribution; nodiv: consolidateRankNoDiv).  Returns |pr_new - pr_old|.
+// The per-vertex inputs are loaded by finish_load, which the work-list
+// kernel issues before its gathers so that their latency overlaps them
+// (and before any store: the arrays are not restrict, so a load after a
+// store would wait for it).
+struct FinishIn {
+    float prev;        // the rank the diff compares against
+    uint32_t dg;       // out-degree
+    uint32_t at;       // where the gathered copy goes (slot or vertex)
+};
+
+template<bool NODIV>
+__device__ __forceinline__ FinishIn finish_load(const PrArgs &a, uint64_t v)
+{
+    FinishIn in;
+    in.prev = NODIV ? a.pr_in[v] : a.pr_out[v];
+    in.dg = a.deg[v];
+    in.at = a.slot ? a.slot[v] : static_cast<uint32_t>(v);
+    return in;
+}
+
+template<bool NODIV>
+__device__ __forceinline__ float finish_store(const PrArgs &a, uint64_t v, float sum, float base_nd, FinishIn in)
+{
+    if constexpr (!NODIV) {
+        const float nr = consolidate_div(sum, a.base_div);
+        a.pr_out[v] = nr;
+        a.contrib_out[in.at] = in.dg ? __fdiv_rn(nr, static_cast<float>(in.dg)) : 0.0f;
+        return fabsf(nr - in.prev);
+    } else {
+        float nr = __fmaf_rn(DAMPING, sum, base_nd);
+        const float d = fabsf(nr - in.prev);
+        if (in.dg != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(in.dg));
+        a.pr_out[v] = nr;
+        if (a.gat_out) a.gat_out[in.at] = nr;
+        return d;
+    }
+}
+
 template<bool NODIV>
 __device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, float sum, float base_nd)
 {
-    if constexpr (!NODIV) {
-        // both loads before the first store: the arrays are not restrict,
-        // so a load after a store would wait for it
-        const float prev = a.pr_out[v];
-        const uint32_t dg = a.deg[v];
-        const uint64_t at = a.slot ? a.slot[v] : v;
-        const float nr = consolidate_div(sum, a.base_div);
-        a.pr_out[v] = nr;
-        a.contrib_out[at] = dg ? __fdiv_rn(nr, static_cast<float>(dg)) : 0.0f;
-        return fabsf(nr - prev);
-    } else {
-        const float prev = a.pr_in[v];
-        const uint32_t dg = a.deg[v];
-        const uint32_t at = a.gat_out ? a.slot[v] : 0u;
-        float nr = __fmaf_rn(DAMPING, sum, base_nd);
-        const float d = fabsf(nr - prev);
-        if (dg != 0 && a.not_last) nr = __fdiv_rn(nr, static_cast<float>(dg));
-        a.pr_out[v] = nr;
-        if (a.gat_out) a.gat_out[at] = nr;
-        return d;
-    }
+    return finish_store<NODIV>(a, v, sum, base_nd, finish_load<NODIV>(a, v));
 }
 
 // ----------------------------- pull variants ------------------------------
@@ -393,7 +411,8 @@ constexpr uint32_t ROW_MASK = 0x3fffffffu;
 constexpr int PULL_WIDE = 1024, PULL_NARROW = 256;
 constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (SEG_EDGES + 33) * sizeof(float); }
 constexpr int pull_min_blocks(int block, bool exact) { return block == PULL_WIDE ? 1 : (exact ? 4 : 5); }
-// default hub-cache entries per block
+// default hub-cache entries per block (measured on GB300: WIDE with 16K
+// entries is within 3% of the best shape on both R-MAT-22 and ER(4M, 67M))
 constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
 constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
@@ -636,8 +655,11 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
         reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
     __syncthreads();
     float dsum = 0.0f;
+    // the next item's descriptor is loaded one item ahead
+    uint4 w_next = warp < a.work_count ? a.work[warp] : make_uint4(0, 0, 0, 0);
     for (uint64_t it = warp; it < a.work_count; it += warps) {
-        const uint4 w = a.work[it];
+        const uint4 w = w_next;
+        if (it + warps < a.work_count) w_next = a.work[it + warps];
         const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
         if (!EXACT_LONG && (w.y & PIECE_FLAG)) {
             float part = 0.0f;
@@ -702,16 +724,21 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
             }
             continue;
         }
-        // up to 32 short rows
+        // up to 32 short rows: lane l owns row r0 + l; its row end and
+        // consolidation inputs are loaded alongside the gathers
         const uint32_t rows = r1 - r0, len = e1 - e0;
-        if (lane < rows) s_end[lane] = a.rev_v[r0 + lane + 1] - e0;
+        FinishIn fin{0.0f, 0u, 0u};
+        if (lane < rows) {
+            s_end[lane] = a.rev_v[r0 + lane + 1] - e0;
+            fin = finish_load<NODIV>(a, r0 + lane);
+        }
         gather_into(ge, src, hub, hubs, e0, len, buf, lane);
         __syncwarp();
         if (lane < rows) {
             const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
             float sum = 0.0f;
             for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
-            dsum += finish_vertex<NODIV>(a, r0 + lane, sum, base_nd);
+            dsum += finish_store<NODIV>(a, r0 + lane, sum, base_nd, fin);
         }
         __syncwarp();
     }
@@ -792,9 +819,9 @@ Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cf
 {
     Geometry g{256, static_cast<unsigned>(ctx->sm_count) * 8, 0};
     if (variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV) {
-        // block_size picks the shape (default NARROW); one resident wave
+        // block_size picks the shape (default WIDE); one resident wave
         const bool exact = variant != PR_PULL_SEGMENTED;
-        g.block = (cfg && cfg->block_size == PULL_WIDE) ? PULL_WIDE : PULL_NARROW;
+        g.block = (cfg && cfg->block_size == PULL_NARROW) ? PULL_NARROW : PULL_WIDE;
         g.grid = static_cast<unsigned>(ctx->sm_count) * pull_min_blocks(static_cast<int>(g.block), exact);
         if (cfg && cfg->grid_size) g.grid = cfg->grid_size;
         g.smem = pull_fixed_smem(static_cast<int>(g.block));  // + the hub cache (run_pagerank)
@@ -1019,7 +1046,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         // hub cache entries per block: chunk_size when given, else the
         // default for the shape; never more than the block's share of
         // shared memory allows
-        const int block = (cfg && cfg->block_size == PULL_WIDE) ? PULL_WIDE : PULL_NARROW;
+        const int block = (cfg && cfg->block_size == PULL_NARROW) ? PULL_NARROW : PULL_WIDE;
         const uint64_t per_sm = block == PULL_WIDE ? 1 : static_cast<uint64_t>(pull_min_blocks(block, need_exact));
         const size_t fixed = pull_fixed_smem(block);
         const size_t share = std::min<size_t>(ctx->max_smem_optin, ctx->max_smem_per_sm / per_sm);
