@@ -359,8 +359,13 @@ class PageRankRun:
     iteration_ms: list = field(default_factory=list)
 
 
-def _cfg(block=0, grid=0, warp=0, chunk=0):
-    return _abi.LaunchConfig(block, grid, warp, chunk)
+def _relabel_flags(relabel):
+    """None: the library decides; True / False force the hub-first order."""
+    return 0 if relabel is None else (_abi.LAUNCH_RELABEL if relabel else _abi.LAUNCH_NO_RELABEL)
+
+
+def _cfg(block=0, grid=0, warp=0, chunk=0, flags=0):
+    return _abi.LaunchConfig(block, grid, warp, chunk, flags)
 
 
 def _stats_list(arr, count):
@@ -422,7 +427,7 @@ def bfs_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], ro
 
 def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int = 30, *,
              ranks=None, block: int = 0, grid: int = 0, warp: int = 0, chunk: int = 0,
-             loop: str = "host", stream=None) -> PageRankRun:
+             relabel: bool | None = None, loop: str = "host", stream=None) -> PageRankRun:
     """PageRank, damping 0.85, 1/N init, exactly `iterations` iterations."""
     torch = _torch()
     lib = library()
@@ -432,7 +437,7 @@ def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int =
     res = _abi.PagerankResult()
     diffs = (C.c_float * max(iterations, 1))()
     rc = lib.bw_pagerank_run(ctx.handle, C.byref(g.view), pagerank_variant_id(variant), iterations,
-                             _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk)),
+                             _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk, _relabel_flags(relabel))),
                              1 if loop == "graph" else 0, C.byref(res), diffs, C.c_void_p(st.cuda_stream))
     check(rc, f"pagerank {variant}")
     return PageRankRun(ranks, res.iterations, res.device_ms, list(diffs)[:iterations])
@@ -440,7 +445,7 @@ def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int =
 
 def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], iterations: int = 30,
                       *, ranks=None, time_iterations: bool = False, block: int = 0, grid: int = 0,
-                      warp: int = 0, chunk: int = 0, stream=None) -> PageRankRun:
+                      warp: int = 0, chunk: int = 0, relabel: bool | None = None, stream=None) -> PageRankRun:
     torch = _torch()
     lib = library()
     sched = [pagerank_variant_id(v) for v in schedule]
@@ -451,7 +456,8 @@ def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int
     res = _abi.PagerankResult()
     it_ms = (C.c_float * max(iterations, 1))()
     rc = lib.bw_pagerank_run_schedule(ctx.handle, C.byref(g.view), arr_s, len(sched), iterations,
-                                      _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk)),
+                                      _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk,
+                                                                _relabel_flags(relabel))),
                                       int(time_iterations), it_ms, C.byref(res), C.c_void_p(st.cuda_stream))
     check(rc, "pagerank schedule")
     run = PageRankRun(ranks, res.iterations, res.device_ms)

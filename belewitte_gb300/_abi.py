@@ -36,7 +36,11 @@ class DeviceGraphC(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("block_size", C.c_uint32), ("grid_size", C.c_uint32),
-                ("warp_size", C.c_uint32), ("chunk_size", C.c_uint32)]
+                ("warp_size", C.c_uint32), ("chunk_size", C.c_uint32), ("flags", C.c_uint32)]
+
+
+LAUNCH_RELABEL = 1
+LAUNCH_NO_RELABEL = 2
 
 
 class BfsLevelStats(C.Structure):

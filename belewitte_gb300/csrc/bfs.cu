@@ -244,7 +244,7 @@ int traversed_edges(bw_context *ctx, const bw_graph_view *g, int32_t *levels, cu
     *out = 0;
     if (!g->fwd_vertices) return BW_OK;
     unsigned long long *d = nullptr;
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&d), sizeof *d, s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&d), sizeof *d, s));
     BW_CUDA(cudaMemsetAsync(d, 0, sizeof *d, s));
     k_traversed<<<ctx->sm_count * 4, 256, 0, s>>>(levels, g->fwd_vertices, g->vertex_count, d);
     unsigned long long h = 0;
@@ -331,7 +331,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
     if (cluster_path) BW_TRY(ensure_outdeg(ctx, g, s));   // frontier edge volumes gate the cluster path
     LevelSlot *log = nullptr;
     const uint32_t log_cap = stats ? std::min(stats_cap, max_levels) : 0;
-    if (log_cap) BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
+    if (log_cap) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;

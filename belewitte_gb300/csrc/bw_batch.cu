@@ -237,7 +237,7 @@ extern "C" int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode, c
     const size_t per_cta = static_cast<size_t>(2) * max_unit_vertices;
     char *scratch = nullptr;
     const size_t bytes = 64 + grid * per_cta * sizeof(uint32_t) + (a.pr_iters ? grid * per_cta * sizeof(float) : 0);
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), bytes, s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&scratch), bytes, s));
     BW_CUDA(cudaMemsetAsync(scratch, 0, 64, s));
     a.cursor = reinterpret_cast<uint32_t *>(scratch);
     a.traversed = reinterpret_cast<unsigned long long *>(scratch + 8);

@@ -207,6 +207,17 @@ int bw_context_create(int device, bw_context **out)
         bw_context_destroy(ctx);
         return BW_ERR_CUDA;
     }
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&ctx->pool, &props) == cudaSuccess) {
+        uint64_t keep = ~uint64_t(0);
+        cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+        ctx->pool = nullptr;                 // fall back to the device's default pool
+        cudaGetLastError();
+    }
     *out = ctx;
     return BW_OK;
 }
@@ -215,6 +226,10 @@ int bw_context_destroy(bw_context *ctx)
 {
     if (!ctx) return BW_OK;
     cudaSetDevice(ctx->device);
+    if (ctx->pool) {
+        cudaDeviceSynchronize();             // scratch frees still queued on streams
+        cudaMemPoolDestroy(ctx->pool);
+    }
     cudaFree(ctx->bfs_ctl);
     if (ctx->bfs_ctl_host) cudaFreeHost(ctx->bfs_ctl_host);
     cudaFree(ctx->queue[0]);

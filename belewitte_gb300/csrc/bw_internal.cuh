@@ -100,6 +100,10 @@ struct bw_context {
     size_t max_smem_per_block = 0;
     size_t max_smem_optin = 0;
     size_t max_smem_per_sm = 0;
+    // Stream-ordered pool for per-run scratch.  Its release threshold is
+    // unbounded, so memory freed at the end of a run is reused by the next
+    // one instead of going back to the driver at every synchronisation.
+    cudaMemPool_t pool = nullptr;
 
     // BFS scratch
     bw::BfsCtl *bfs_ctl = nullptr;        // device
@@ -157,3 +161,9 @@ void compute_division(uint64_t count, uint32_t sm, uint32_t max_tpb,
                       uint32_t *block, uint32_t *grid);
 
 }  // namespace bw
+
+// Stream-ordered scratch from the context's pool.
+inline cudaError_t ctx_malloc_async(bw_context *ctx, void **p, size_t bytes, cudaStream_t s)
+{
+    return ctx && ctx->pool ? cudaMallocFromPoolAsync(p, bytes, ctx->pool, s) : cudaMallocAsync(p, bytes, s);
+}

@@ -493,7 +493,7 @@ int bw_mlp_train(bw_context *ctx, float *params, uint32_t classes, const float *
     a.steps = cfg->steps; a.batch = cfg->batch; a.lr = cfg->lr; a.b1 = cfg->beta1; a.b2 = cfg->beta2;
     a.eps = cfg->eps; a.wd = cfg->weight_decay; a.seed = cfg->seed; a.points = loss_curve ? loss_points : 0;
     float *scratch = nullptr;
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (2 * P + a.points + 1) * sizeof(float), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&scratch), (2 * P + a.points + 1) * sizeof(float), s));
     BW_CUDA(cudaMemsetAsync(scratch, 0, (2 * P + a.points + 1) * sizeof(float), s));
     a.adam_m = scratch; a.adam_v = scratch + P; a.loss_curve = scratch + 2 * P;
     const size_t smem = train_smem_bytes(classes);
@@ -513,7 +513,7 @@ int bw_mlp_gradient(bw_context *ctx, const float *params, uint32_t classes, cons
         return BW_ERR_INVALID_ARGUMENT;
     cudaStream_t s = as_stream(stream);
     float *dloss = nullptr;
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&dloss), sizeof(float), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&dloss), sizeof(float), s));
     const size_t smem = train_smem_bytes(classes);
     BW_CUDA(cudaFuncSetAttribute(k_mlp_gradient, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     k_mlp_gradient<<<1, TRAIN_THREADS, smem, s>>>(params, classes, X, T, W, n, grad, dloss);
@@ -558,7 +558,7 @@ int bw_bfs_profile(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32
     if (sample_every == 0) sample_every = 1;
     const uint64_t n = g->vertex_count, m = g->edge_count;
     BfsCtl *ctl_snap = nullptr;
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&ctl_snap), sizeof(BfsCtl), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&ctl_snap), sizeof(BfsCtl), s));
     BW_TRY(ensure_level_events(ctx, 2));
     k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, s>>>(levels, n, root, ctx->queue[0], ctx->bfs_ctl, max_levels,
                                                      ctx->outdeg);
@@ -697,7 +697,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
     // Device loop: WHILE { predict -> SWITCH(K level bodies) -> step }.
     LevelSlot *log = nullptr;
     const uint32_t log_cap = stats ? std::min(stats_cap, max_levels) : 0;
-    if (log_cap) BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
+    if (log_cap) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int rc = BW_OK;

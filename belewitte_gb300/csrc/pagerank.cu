@@ -170,6 +170,31 @@ __global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint64_t n, uin
     }
 }
 
+// Edges covered by the first `k` entries in degree order and in vertex
+// order (one block).
+__global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ order,
+                                   uint64_t k, unsigned long long *out)
+{
+    __shared__ unsigned long long part[2][32];
+    unsigned long long sorted = 0, natural = 0;
+    for (uint64_t i = threadIdx.x; i < k; i += blockDim.x) {
+        sorted += deg[order[i]];
+        natural += deg[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sorted += __shfl_xor_sync(FULL_MASK, sorted, o);
+        natural += __shfl_xor_sync(FULL_MASK, natural, o);
+    }
+    if ((threadIdx.x & 31) == 0) { part[0][threadIdx.x >> 5] = sorted; part[1][threadIdx.x >> 5] = natural; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = 0, b = 0;
+        for (unsigned w = 0; w < blockDim.x / 32; w++) { a += part[0][w]; b += part[1][w]; }
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
 __global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, uint32_t *__restrict__ slot)
 {
     for (uint64_t i = gtid(); i < n; i += gthreads()) slot[order[i]] = static_cast<uint32_t>(i);
@@ -745,43 +770,6 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
     add_diff(a.diff, dsum);
 }
 
-__global__ void k_exclusive_scan_small(uint32_t *data, uint64_t count, uint32_t *total)
-{
-    // single block scan used for the work-item layout (count = 2 x N/32)
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint64_t base = 0; base < count; base += blockDim.x) {
-        const uint64_t i = base + threadIdx.x;
-        uint32_t x = i < count ? data[i] : 0;
-        // block inclusive scan via warp scans
-        __shared__ uint32_t warp_tot[32];
-        const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        uint32_t incl = x;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
-            if (lane >= static_cast<unsigned>(o)) incl += y;
-        }
-        if (lane == 31) warp_tot[wid] = incl;
-        __syncthreads();
-        if (wid == 0) {
-            uint32_t t = lane < (blockDim.x >> 5) ? warp_tot[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL_MASK, t, o);
-                if (lane >= static_cast<unsigned>(o)) t += y;
-            }
-            warp_tot[lane] = t;
-        }
-        __syncthreads();
-        const uint32_t before = (wid ? warp_tot[wid - 1] : 0) + carry;
-        if (i < count) data[i] = before + incl - x;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = before + incl;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = carry;
-}
-
 }  // namespace
 }  // namespace bw
 
@@ -868,6 +856,13 @@ int validate_cfg(const bw_context *ctx, int variant, const bw_launch_config *cfg
 int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t *deg, cudaStream_t s)
 {
     if (uses_rowlen(variant)) return BW_OK;   // push variants use the row length
+    if (g->fwd_vertices) {
+        // the forward CSR's row lengths are the counts the reference's
+        // degree kernels produce, at the cost of one pass over N
+        k_row_lengths<<<ctx->sm_count * 4, 256, 0, s>>>(g->fwd_vertices, g->vertex_count, deg);
+        BW_CUDA(cudaGetLastError());
+        return BW_OK;
+    }
     BW_CUDA(cudaMemsetAsync(deg, 0, g->vertex_count * sizeof(uint32_t), s));  // zeroInitDegreesKernel
     if (g->edge_count == 0) return BW_OK;
     const unsigned grid = ctx->sm_count * 8;
@@ -894,12 +889,21 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     // Row groups <= N; pieces <= M / SEG_EDGES + (rows longer than
     // SEG_LONG) <= M / SEG_EDGES + M / SEG_LONG.
     const uint64_t cap = windows + n + g->edge_count / SEG_EDGES + g->edge_count / SEG_LONG + 16;
-    // counts: [pieces of window 0..W-1 | short items of window 0..W-1 | total]
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.win_counts), (2 * windows + 1) * sizeof(uint32_t), s));
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
-    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, run.win_counts);
-    k_exclusive_scan_small<<<1, 1024, 0, s>>>(run.win_counts, 2 * windows, run.win_counts + 2 * windows);
+    // counts: [pieces of window 0..W-1 | short items of window 0..W-1 | 0],
+    // scanned in place into first positions (the last entry: the total)
+    const uint64_t entries = 2 * windows + 1;
+    size_t temp = 0;
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp, static_cast<uint32_t *>(nullptr),
+                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(entries), s));
+    const uint64_t temp_at = (2 * entries + 63) & ~uint64_t(63);   // 256-byte aligned scan storage
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.win_counts), temp_at * sizeof(uint32_t) + temp, s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
+    uint32_t *counts = run.win_counts + entries;
+    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, counts);
+    BW_CUDA(cudaMemsetAsync(counts + 2 * windows, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(run.win_counts + temp_at, temp, counts, run.win_counts,
+                                          static_cast<int64_t>(entries), s));
     k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts, run.work, run.long_count);
     BW_CUDA(cudaGetLastError());
     uint32_t totals[2] = {0, 0};       // pieces (the exclusive prefix at W), all items
@@ -908,7 +912,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     BW_CUDA(cudaStreamSynchronize(s));
     run.work_count = totals[1];
     if (!split && totals[0])
-        BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&run.vals), g->edge_count * sizeof(float), s));
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), g->edge_count * sizeof(float), s));
     return BW_OK;
 }
 
@@ -962,22 +966,37 @@ struct Relabel {
 
 // Orders vertices by decreasing out-degree class (floor(log2(deg))), stable
 // in vertex order, and translates the reverse CSR's sources (one pass over
-// M).  Runs after the degrees, inside the timed region.
-int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, Relabel &r, cudaStream_t s)
+// M).  Runs after the degrees, inside the timed region.  Unless `force`,
+// it stops after the (cheap) ordering when the first `hubs` entries would
+// cover less than 5% more of the edges than in vertex order; `used` tells.
+int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, uint32_t hubs, bool force,
+                  Relabel &r, bool &used, cudaStream_t s)
 {
+    used = false;
     const uint64_t n = g->vertex_count, m = g->edge_count;
     size_t temp = 0;
     cub::DoubleBuffer<uint32_t> keys(nullptr, nullptr), ids(nullptr, nullptr);
     BW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
     const size_t words = 4 * n, temp_words = (temp + 3) / 4;
-    BW_CUDA(cudaMallocAsync(&r.scratch, (words + temp_words) * sizeof(uint32_t), s));
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
-    BW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
+    const size_t cov_at = (words + temp_words + 1) & ~size_t(1);       // two 64-bit counters after the sort
+    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (cov_at + 4) * sizeof(uint32_t), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
     uint32_t *base = static_cast<uint32_t *>(r.scratch);
     keys = cub::DoubleBuffer<uint32_t>(base, base + n);
     ids = cub::DoubleBuffer<uint32_t>(base + 2 * n, base + 3 * n);
     k_relabel_keys<<<ctx->sm_count * 4, 256, 0, s>>>(deg, n, keys.Current(), ids.Current());
     BW_CUDA(cub::DeviceRadixSort::SortPairs(base + words, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
+    if (!force) {
+        unsigned long long *cov = reinterpret_cast<unsigned long long *>(base + cov_at);
+        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, ids.Current(), std::min<uint64_t>(hubs, n), cov);
+        unsigned long long host_cov[2] = {0, 0};
+        BW_CUDA(cudaMemcpyAsync(host_cov, cov, sizeof host_cov, cudaMemcpyDeviceToHost, s));
+        BW_CUDA(cudaStreamSynchronize(s));
+        if (static_cast<double>(host_cov[0]) - static_cast<double>(host_cov[1]) < 0.05 * static_cast<double>(m))
+            return BW_OK;
+    }
+    used = true;
     k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.slot);
     if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.slot, r.gat_e);
     BW_CUDA(cudaGetLastError());
@@ -991,11 +1010,6 @@ void free_relabel(Relabel &r, cudaStream_t s)
     if (r.gat_e) cudaFreeAsync(r.gat_e, s);
     r = Relabel{};
 }
-
-// Hub-first order pays when the work-list kernels run several iterations
-// over a graph whose gathered array is larger than L1 many times over.
-constexpr uint64_t RELABEL_MIN_VERTICES = 1u << 16;
-constexpr uint32_t RELABEL_MIN_ITERATIONS = 3;
 
 // Runs a (possibly switching) schedule of variants of one semantics class.
 int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
@@ -1077,18 +1091,22 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     }
     BW_CUDA(cudaMemsetAsync(ctx->pr_diffs, 0, (iterations + 1) * sizeof(float), s));
     Relabel rl;
-    const bool relabel = all_items && n >= RELABEL_MIN_VERTICES && iterations >= RELABEL_MIN_ITERATIONS &&
-                         g->edge_count > 0;
-    if (relabel) {
-        const int rc = build_relabel(ctx, g, ctx->pr_deg, rl, s);
+    const uint32_t flags = cfg ? cfg->flags : 0u;
+    const bool force = (flags & BW_LAUNCH_RELABEL) != 0;
+    bool relabel = false;
+    if (all_items && g->edge_count > 0 && !(flags & BW_LAUNCH_NO_RELABEL) &&
+        (force || (iterations >= 4 && a.hub_count > 0))) {
+        const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, relabel, s);
         if (rc != BW_OK) {
             free_relabel(rl, s);
             free_run(split_run, s);
             free_run(exact_run, s);
             return rc;
         }
-        a.slot = rl.slot;
-        a.gat_e = rl.gat_e;
+        if (relabel) {
+            a.slot = rl.slot;
+            a.gat_e = rl.gat_e;
+        }
     }
     // nodiv + relabelled sources: the gathered copy of the ranks, in slot order
     float *gat[2] = {ctx->pr_buf[1], ctx->pr_acc};

@@ -207,7 +207,23 @@ typedef struct bw_launch_config {
     uint32_t grid_size;
     uint32_t warp_size;
     uint32_t chunk_size;
+    uint32_t flags;               /* BW_LAUNCH_* (no reference counterpart) */
 } bw_launch_config;
+
+/*
+ * Work-list PageRank variants (vertex-pull, vertex-pull-nodiv,
+ * pull-segmented): block_size 1024 (default) or 256 picks the block shape,
+ * chunk_size the number of gathered-array entries each block caches in
+ * shared memory (0 = default, multiple of 4).  Relabelling stores the
+ * gathered array in decreasing out-degree order so that the cached entries
+ * are the hubs; it costs one pass over the edges per run and leaves every
+ * result unchanged.  By default it runs when the cached entries would cover
+ * at least 5% more of the edges than in vertex order (and the run has at
+ * least 4 iterations); BW_LAUNCH_RELABEL forces it, BW_LAUNCH_NO_RELABEL
+ * turns it off.
+ */
+#define BW_LAUNCH_RELABEL 1u
+#define BW_LAUNCH_NO_RELABEL 2u
 
 /* Reference Backend::computeDivision for `count` items. */
 void bw_compute_division(uint64_t count, uint32_t sm_count,

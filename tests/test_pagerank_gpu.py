@@ -100,12 +100,14 @@ def test_long_rows(ctx, long_graphs, variant, iterations):
 
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
 @pytest.mark.parametrize("block,hubs", [(256, 0), (256, 4), (256, 2048), (1024, 0), (1024, 16384), (1024, 1 << 20)])
-def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs):
+@pytest.mark.parametrize("relabel", [False, True])
+def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs, relabel):
     """Both block shapes of the work-list kernels, with and without the
     shared-memory hub cache (sizes beyond the graph or the shared memory
-    are clamped): results do not depend on the shape."""
+    are clamped) and the hub-first source order: results do not depend on
+    any of them."""
     for name, (h, g) in list(long_graphs.items()) + [("rmat14", graphs["rmat14"]), ("chain", graphs["chain"])]:
-        got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs).ranks.cpu().numpy()
+        got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs, relabel=relabel).ranks.cpu().numpy()
         div, nodiv, _, _ = _oracles(h, 30)
         ref = nodiv if "nodiv" in variant else div
         if variant in BITEXACT:
