@@ -103,6 +103,21 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _profiled_traffic(variant: str):
+    """DRAM bytes per launch of the variant's iteration kernel on this
+    workload, from the committed ncu summary (None when there is none)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                        f"pagerank_{variant.replace('-', '_')}_rmat{SCALE}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def _measured_peak():
     try:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
@@ -369,7 +384,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (graph %.0f MB > 129 MB)" % ((4 * (n + 1) + 4 * m) / 1e6),
                    "parallelism": f"independent replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4), "traffic": _profiled_traffic(variant),
                      "kernel": DOMINANT.get(variant, "k_pr_edge"), "kernel_ms": round(kernel_ms, 5),
                      "algorithmic_bytes": ab, "peak_source": peak_kind},
         "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d,
