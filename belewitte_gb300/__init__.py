@@ -357,6 +357,7 @@ class PageRankRun:
     device_ms: float
     diffs: list = field(default_factory=list)
     iteration_ms: list = field(default_factory=list)
+    kernel_launches: int = 0  # this library's kernels the run launched
 
 
 def _relabel_flags(relabel):
@@ -440,7 +441,8 @@ def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int =
                              _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk, _relabel_flags(relabel))),
                              1 if loop == "graph" else 0, C.byref(res), diffs, C.c_void_p(st.cuda_stream))
     check(rc, f"pagerank {variant}")
-    return PageRankRun(ranks, res.iterations, res.device_ms, list(diffs)[:iterations])
+    return PageRankRun(ranks, res.iterations, res.device_ms, list(diffs)[:iterations],
+                       kernel_launches=res.kernel_launches)
 
 
 def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], iterations: int = 30,
@@ -460,7 +462,7 @@ def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int
                                                                 _relabel_flags(relabel))),
                                       int(time_iterations), it_ms, C.byref(res), C.c_void_p(st.cuda_stream))
     check(rc, "pagerank schedule")
-    run = PageRankRun(ranks, res.iterations, res.device_ms)
+    run = PageRankRun(ranks, res.iterations, res.device_ms, kernel_launches=res.kernel_launches)
     if time_iterations:
         run.iteration_ms = list(it_ms)[:iterations]
     return run

@@ -57,7 +57,7 @@ class BfsResult(C.Structure):
 
 
 class PagerankResult(C.Structure):
-    _fields_ = [("iterations", C.c_uint32), ("reserved", C.c_uint32),
+    _fields_ = [("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
                 ("last_diff", C.c_float), ("reserved_f", C.c_float),
                 ("device_ms", C.c_double)]
 

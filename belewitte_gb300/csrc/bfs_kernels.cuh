@@ -531,6 +531,82 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
 // ---------------------------------------------------------------------------
 constexpr uint32_t CLUSTER_CAP = 65536;            // frontier vertices
 constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;   // frontier out-edges
+constexpr uint32_t CLUSTER_STAGE = 8192;           // next-frontier entries staged per block
+
+// Per-level accumulators of one block of the cluster kernel: every thread
+// counts locally, the block reduces once per level and issues one global
+// atomic per counter (per-warp atomics on the shared level slot serialise
+// at L2 and dominated short levels).  Newly visited vertices are staged in
+// shared memory and copied to the global next-frontier queue in one block
+// once the level is done; entries beyond the stage go to the queue directly.
+template<bool SIDE>
+struct ClusterLevel {
+    uint32_t hits = 0;
+    unsigned long long fe = 0;
+    float ls = 0.f, lq = 0.f, lm = 0.f;
+
+    __device__ __forceinline__ void visit(const BfsArgs &a, uint32_t *stage, uint32_t *stage_n, uint32_t *qnext,
+                                          LevelSlot *slot, uint32_t v)
+    {
+        hits++;
+        cg::coalesced_group g = cg::coalesced_threads();
+        uint32_t base = 0;
+        if (g.thread_rank() == 0) base = atomicAdd(stage_n, g.size());
+        base = g.shfl(base, 0) + g.thread_rank();
+        if (base < CLUSTER_STAGE) stage[base] = v;
+        else queue_append(qnext, &slot->qlen, v);
+        const uint32_t d = a.outdeg[v];
+        fe += d;
+        if constexpr (SIDE) {
+            const float l = __log2f(1.0f + static_cast<float>(d));
+            ls += l; lq += l * l; lm = fmaxf(lm, l);
+        }
+    }
+
+    // Every thread of the block calls; ends with the staged entries in the
+    // global queue and the level's counters in `slot`.
+    __device__ __forceinline__ void finish(uint32_t *stage, uint32_t *stage_n, uint32_t *qnext, LevelSlot *slot)
+    {
+        __shared__ unsigned long long r_fe[CLUSTER_THREADS / 32];
+        __shared__ uint32_t r_hits[CLUSTER_THREADS / 32];
+        __shared__ float r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32], r_lm[CLUSTER_THREADS / 32];
+        __shared__ uint32_t q_base;
+        const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = 16; o > 0; o >>= 1) {
+            hits += __shfl_xor_sync(FULL_MASK, hits, o);
+            fe += __shfl_xor_sync(FULL_MASK, fe, o);
+            if constexpr (SIDE) {
+                ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+            }
+        }
+        if (lane == 0) { r_hits[wid] = hits; r_fe[wid] = fe; r_ls[wid] = ls; r_lq[wid] = lq; r_lm[wid] = lm; }
+        __syncthreads();
+        const uint32_t staged = min(*stage_n, CLUSTER_STAGE);
+        if (threadIdx.x == 0) {
+            uint32_t h = 0;
+            unsigned long long e = 0;
+            float s1 = 0.f, s2 = 0.f, mx = 0.f;
+            for (unsigned w = 0; w < CLUSTER_THREADS / 32; w++) {
+                h += r_hits[w]; e += r_fe[w]; s1 += r_ls[w]; s2 += r_lq[w]; mx = fmaxf(mx, r_lm[w]);
+            }
+            if (h) atomicAdd(&slot->frontier, h);
+            if (e) atomicAdd(&slot->fedges, e);
+            if constexpr (SIDE) {
+                if (h) {
+                    atomicAdd(&slot->lsum, s1);
+                    atomicAdd(&slot->lsq, s2);
+                    atomicMax(&slot->lmax_bits, __float_as_uint(mx));
+                }
+            }
+            q_base = staged ? atomicAdd(&slot->qlen, staged) : 0u;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) qnext[q_base + i] = stage[i];
+        hits = 0; fe = 0; ls = lq = lm = 0.f;
+    }
+};
 
 template<bool SIDE>
 __global__ void __cluster_dims__(CLUSTER_CTAS, 1, 1) __launch_bounds__(CLUSTER_THREADS)
@@ -538,6 +614,8 @@ k_bfs_cluster(BfsArgs a)
 {
     __shared__ uint32_t s_excl[CLUSTER_THREADS / 32][32];
     __shared__ uint32_t s_start[CLUSTER_THREADS / 32][32];
+    __shared__ uint32_t s_stage[CLUSTER_STAGE];
+    __shared__ uint32_t s_stage_n;
     cg::cluster_group cl = cg::this_cluster();
     BfsCtl *ctl = a.ctl;
     const unsigned rank = cl.block_rank();
@@ -553,15 +631,15 @@ k_bfs_cluster(BfsArgs a)
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = uint64_t(rank) * (CLUSTER_THREADS / 32) + wib;
     const uint64_t warps = uint64_t(CLUSTER_CTAS) * (CLUSTER_THREADS / 32);
+    ClusterLevel<SIDE> acc;
     for (;;) {
         const int32_t nd = L + 1;
         LevelSlot *slot = &ctl->slot[L % 3];
         if (leader) reset_slot(&ctl->slot[(L + 1) % 3]);
+        if (threadIdx.x == 0) s_stage_n = 0;
+        __syncthreads();
         const uint32_t *qin = (L & 1) ? a.q1 : a.q0;
         uint32_t *qnext = (L & 1) ? a.q0 : a.q1;
-        Counter<RED_WARP> cnt;
-        Side<SIDE> side;
-        unsigned long long fe = 0;
         for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
             const uint64_t i = t + lane;
             uint32_t v = 0, s = 0, d = 0;
@@ -592,40 +670,25 @@ k_bfs_cluster(BfsArgs a)
                     if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
                 }
                 const uint32_t u = __ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo]));
-                if (relax(lv, u, nd)) {
-                    cnt.hit(&slot->frontier);
-                    queue_append(qnext, &slot->qlen, u);
-                    if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
-                    else fe += a.outdeg[u];
-                }
+                if (relax(lv, u, nd)) acc.visit(a, s_stage, &s_stage_n, qnext, slot, u);
             }
             __syncwarp();
         }
-        cnt.finish(&slot->frontier);
-        side.finish(slot);
-        if constexpr (!SIDE) flush_edges(slot, fe);
+        acc.finish(s_stage, &s_stage_n, qnext, slot);
         cl.sync();
         const uint32_t chunks = __ldcg(&slot->heavy);
         if (chunks) {                                      // hub chunks: a second phase
-            Counter<RED_WARP> cnt2;
-            Side<SIDE> side2;
-            unsigned long long fe2 = 0;
+            if (threadIdx.x == 0) s_stage_n = 0;
+            __syncthreads();
             for (uint64_t c = warp; c < chunks; c += warps) {
                 const uint2 h = __ldcg(a.heavy + c);
                 const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
                 for (uint32_t i = h.y + lane; i < end; i += 32) {
                     const uint32_t u = __ldg(a.fwd_e + i);
-                    if (relax(lv, u, nd)) {
-                        cnt2.hit(&slot->frontier);
-                        queue_append(qnext, &slot->qlen, u);
-                        if constexpr (SIDE) side2.visit(a, nullptr, nullptr, u);
-                        else fe2 += a.outdeg[u];
-                    }
+                    if (relax(lv, u, nd)) acc.visit(a, s_stage, &s_stage_n, qnext, slot, u);
                 }
             }
-            cnt2.finish(&slot->frontier);
-            side2.finish(slot);
-            if constexpr (!SIDE) flush_edges(slot, fe2);
+            acc.finish(s_stage, &s_stage_n, qnext, slot);
             cl.sync();
         }
         const uint32_t f = __ldcg(&slot->qlen);

@@ -81,20 +81,18 @@ __global__ void k_row_lengths(const uint32_t *__restrict__ off, uint64_t n,
         deg[v] = off[v + 1] - off[v];
 }
 
+// Out-degrees of the view's graph, recomputed for every run (one pass over
+// N): a cache keyed on the offsets pointer went stale when a freed graph's
+// memory was reused by another graph of the same size.
 int ensure_outdeg(bw_context *ctx, const bw_graph_view *g, cudaStream_t s)
 {
     if (!g->fwd_vertices) return BW_ERR_MISSING_REPRESENTATION;
     if (g->vertex_count > ctx->outdeg_cap) {
         BW_TRY(grow(&ctx->outdeg, g->vertex_count));
         ctx->outdeg_cap = g->vertex_count;
-        ctx->outdeg_key = nullptr;
     }
-    if (ctx->outdeg_key != g->fwd_vertices || ctx->outdeg_key_n != g->vertex_count) {
-        k_row_lengths<<<default_grid(ctx, 4), 256, 0, s>>>(g->fwd_vertices, g->vertex_count, ctx->outdeg);
-        BW_CUDA(cudaGetLastError());
-        ctx->outdeg_key = g->fwd_vertices;
-        ctx->outdeg_key_n = g->vertex_count;
-    }
+    k_row_lengths<<<default_grid(ctx, 4), 256, 0, s>>>(g->fwd_vertices, g->vertex_count, ctx->outdeg);
+    BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
 

@@ -104,6 +104,7 @@ struct bw_context {
     // unbounded, so memory freed at the end of a run is reused by the next
     // one instead of going back to the driver at every synchronisation.
     cudaMemPool_t pool = nullptr;
+    uint32_t launches = 0;                // own kernels launched by the current run
 
     // BFS scratch
     bw::BfsCtl *bfs_ctl = nullptr;        // device
@@ -113,8 +114,6 @@ struct bw_context {
     uint64_t bfs_n_cap = 0, heavy_cap = 0;
     uint32_t *outdeg = nullptr;
     uint64_t outdeg_cap = 0;
-    const uint32_t *outdeg_key = nullptr; // fwd_vertices the degrees belong to
-    uint64_t outdeg_key_n = 0;
 
     // PageRank scratch
     float *pr_acc = nullptr, *pr_buf[2] = {nullptr, nullptr};

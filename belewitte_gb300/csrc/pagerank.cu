@@ -860,6 +860,7 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
         // the forward CSR's row lengths are the counts the reference's
         // degree kernels produce, at the cost of one pass over N
         k_row_lengths<<<ctx->sm_count * 4, 256, 0, s>>>(g->fwd_vertices, g->vertex_count, deg);
+        ctx->launches++;
         BW_CUDA(cudaGetLastError());
         return BW_OK;
     }
@@ -878,6 +879,7 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
       default:                     // reverseCSRComputeDegrees
         k_count_ids<<<grid, 256, 0, s>>>(g->rev_edges, g->edge_count, 1, deg); break;
     }
+    ctx->launches++;
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
@@ -905,6 +907,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     BW_CUDA(cub::DeviceScan::ExclusiveSum(run.win_counts + temp_at, temp, counts, run.win_counts,
                                           static_cast<int64_t>(entries), s));
     k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts, run.work, run.long_count);
+    ctx->launches += 2;                  // k_seg_count, k_seg_emit (the scan is the library's)
     BW_CUDA(cudaGetLastError());
     uint32_t totals[2] = {0, 0};       // pieces (the exclusive prefix at W), all items
     BW_CUDA(cudaMemcpyAsync(&totals[0], run.win_counts + windows, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -950,8 +953,10 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         break;
       default: return BW_ERR_UNKNOWN_VARIANT;
     }
+    ctx->launches++;
     if (!is_fused(variant)) {
         k_consolidate_div<<<ctx->sm_count * 8, 256, 0, s>>>(a, uses_rowlen(variant) ? 1 : 0);
+        ctx->launches++;
     }
     BW_CUDA(cudaGetLastError());
     return BW_OK;
@@ -986,10 +991,12 @@ int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, 
     keys = cub::DoubleBuffer<uint32_t>(base, base + n);
     ids = cub::DoubleBuffer<uint32_t>(base + 2 * n, base + 3 * n);
     k_relabel_keys<<<ctx->sm_count * 4, 256, 0, s>>>(deg, n, keys.Current(), ids.Current());
+    ctx->launches++;
     BW_CUDA(cub::DeviceRadixSort::SortPairs(base + words, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
     if (!force) {
         unsigned long long *cov = reinterpret_cast<unsigned long long *>(base + cov_at);
         k_relabel_coverage<<<1, 1024, 0, s>>>(deg, ids.Current(), std::min<uint64_t>(hubs, n), cov);
+        ctx->launches++;
         unsigned long long host_cov[2] = {0, 0};
         BW_CUDA(cudaMemcpyAsync(host_cov, cov, sizeof host_cov, cudaMemcpyDeviceToHost, s));
         BW_CUDA(cudaStreamSynchronize(s));
@@ -999,6 +1006,7 @@ int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, 
     used = true;
     k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.slot);
     if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.slot, r.gat_e);
+    ctx->launches += m ? 2 : 1;
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
@@ -1040,6 +1048,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     cudaStream_t s = as_stream(stream);
     const uint64_t n = g->vertex_count;
     BW_TRY(ensure_pr_scratch(ctx, n, iterations));
+    ctx->launches = 0;
     if (time_iterations) BW_TRY(ensure_level_events(ctx, iterations + 1));
 
     PrRun split_run, exact_run;
@@ -1088,6 +1097,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     if (any_rowlen && any_deg) {
         // mixed schedule: make the degree buffer valid for every variant
         k_row_lengths<<<ctx->sm_count * 4, 256, 0, s>>>(g->fwd_vertices, n, ctx->pr_deg);
+        ctx->launches++;
     }
     BW_CUDA(cudaMemsetAsync(ctx->pr_diffs, 0, (iterations + 1) * sizeof(float), s));
     Relabel rl;
@@ -1124,6 +1134,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     const int first_rowlen = uses_rowlen(schedule[0]) && !any_deg ? 1 : 0;
     k_pr_init<<<ctx->sm_count * 4, 256, 0, s>>>(a, nodiv ? nb[0] : ranks, nodiv ? nullptr : contrib[0],
                                                  nodiv_gat ? gat[0] : nullptr, first_rowlen);
+    ctx->launches++;
     BW_CUDA(cudaGetLastError());
 
     for (uint32_t j = 1; j <= iterations; j++) {
@@ -1178,6 +1189,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         float ms = 0.0f;
         BW_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
         result->iterations = iterations;
+        result->kernel_launches = ctx->launches;
         result->last_diff = diffs_dev_last;
         result->device_ms = ms;
     }

@@ -132,18 +132,9 @@ def _measured_peak():
 # --variant measures another one.
 HEADLINE_VARIANT = "pull-segmented"
 
-FUSED = ("vertex-pull", "vertex-pull-warp", "vertex-pull-nodiv", "vertex-pull-warp-nodiv", "pull-segmented")
-ITEM_LISTS = ("vertex-pull", "vertex-pull-nodiv", "pull-segmented")
 DOMINANT = {"pull-segmented": "k_pr_pull_items", "vertex-pull": "k_pr_pull_items", "vertex-pull-nodiv": "k_pr_pull_items",
             "vertex-pull-warp": "k_pr_vertex_pull_warp", "vertex-pull-warp-nodiv": "k_pr_vertex_pull_warp",
             "vertex-push": "k_pr_vertex_push", "vertex-push-warp": "k_pr_vertex_push_warp"}
-
-
-def pagerank_launches(variant: str, iterations: int) -> int:
-    """Kernels of ours one bw_pagerank_run launches (memsets not counted)."""
-    deg = 0 if variant in ("vertex-push", "vertex-push-warp") else 1
-    seg = 3 if variant in ITEM_LISTS else 0
-    return deg + seg + 1 + iterations * (1 if variant in FUSED else 2)
 
 
 def alg_bytes(variant: str, n: int, m: int) -> int:
@@ -319,9 +310,11 @@ def run_ours(args):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
+        launches = 0
         for _ in range(args.steps):
             run = bw.pagerank_schedule(ctx, g, [variant], ITERATIONS, ranks=ranks, time_iterations=True)
             iter_ms.extend(run.iteration_ms)
+            launches += run.kernel_launches
         t1.record(stream)
         torch.cuda.synchronize()
     if ws > 1:
@@ -389,7 +382,7 @@ def run_ours(args):
                      "algorithmic_bytes": ab, "peak_source": peak_kind},
         "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n * 4)},
-        "gpu_launches": pagerank_launches(variant, ITERATIONS) * args.steps,
+        "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
     result.update(extras)

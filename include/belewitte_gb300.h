@@ -347,7 +347,7 @@ int bw_pagerank_variant_reps(int variant);
 
 typedef struct bw_pagerank_result {
     uint32_t iterations;
-    uint32_t reserved;
+    uint32_t kernel_launches; /* this library's kernels launched by the run */
     float last_diff;        /* sum |pr_new - pr_old| of the last iteration */
     float reserved_f;
     double device_ms;       /* degrees + all iterations on the device */
