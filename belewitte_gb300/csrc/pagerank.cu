@@ -83,6 +83,10 @@ struct PrArgs {
     const uint32_t *gat_e;
     const uint32_t *slot;
     uint32_t hub_count;        // work-list kernels: gathered entries cached in shared memory
+    const uint32_t *rows;      // work-list kernels: rows with in-edges, then rows without
+    // Decided on the device, so the host never waits inside a run:
+    const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
+    const uint32_t *count_dev;    // work-list length (nullptr: work_count)
     const float *gat_in;
     float *gat_out;
     double base_div;           // (1.0 - 0.85f) / N, computed once on the host
@@ -90,6 +94,18 @@ struct PrArgs {
 
 __device__ __forceinline__ uint64_t gtid() { return blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; }
 __device__ __forceinline__ uint64_t gthreads() { return uint64_t(gridDim.x) * blockDim.x; }
+
+// Applies the decisions taken on the device to a kernel's copy of the args.
+__device__ __forceinline__ void resolve_args(PrArgs &a)
+{
+    if (a.relabel_on && *a.relabel_on == 0) {
+        a.slot = nullptr;
+        a.gat_e = a.rev_e;
+        a.gat_in = nullptr;
+        a.gat_out = nullptr;
+    }
+    if (a.count_dev) a.work_count = *a.count_dev;
+}
 
 // pagerank/pagerank.cu:132: new_rank = (float)(((1.0 - d) / N) + (double)(d * acc))
 // -- a double base term (computed once: IEEE division is correctly rounded,
@@ -142,6 +158,8 @@ __global__ void __launch_bounds__(256) k_count_ids(const uint32_t *__restrict__ 
 // relabelled copy of the ranks).
 __global__ void k_pr_init(PrArgs a, float *pr, float *contrib, float *gat, int rowlen)
 {
+    resolve_args(a);
+    if (!a.slot) gat = nullptr;                   // the relabelled copy is not used
     const float init = __fdiv_rn(1.0f, static_cast<float>(a.n));
     for (uint64_t v = gtid(); v < a.n; v += gthreads()) {
         pr[v] = init;
@@ -173,7 +191,7 @@ __global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint64_t n, uin
 // Edges covered by the first `k` entries in degree order and in vertex
 // order (one block).
 __global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ order,
-                                   uint64_t k, unsigned long long *out)
+                                   uint64_t k, uint64_t m, uint32_t *on)
 {
     __shared__ unsigned long long part[2][32];
     unsigned long long sorted = 0, natural = 0;
@@ -190,19 +208,23 @@ __global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint3
     if (threadIdx.x == 0) {
         unsigned long long a = 0, b = 0;
         for (unsigned w = 0; w < blockDim.x / 32; w++) { a += part[0][w]; b += part[1][w]; }
-        out[0] = a;
-        out[1] = b;
+        // worth a pass over the edges: >= 5% more of them on the cached hubs
+        *on = (static_cast<double>(a) - static_cast<double>(b) >= 0.05 * static_cast<double>(m)) ? 1u : 0u;
     }
 }
 
-__global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, uint32_t *__restrict__ slot)
+__global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, const uint32_t *on,
+                                uint32_t *__restrict__ slot)
 {
+    if (*on == 0) return;
     for (uint64_t i = gtid(); i < n; i += gthreads()) slot[order[i]] = static_cast<uint32_t>(i);
 }
 
 __global__ void __launch_bounds__(256) k_relabel_edges(const uint32_t *__restrict__ src, uint64_t m,
-                                                       const uint32_t *__restrict__ slot, uint32_t *__restrict__ out)
+                                                       const uint32_t *on, const uint32_t *__restrict__ slot,
+                                                       uint32_t *__restrict__ out)
 {
+    if (*on == 0) return;
     const uint64_t quads = m / 4;
     const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
     uint4 *o4 = reinterpret_cast<uint4 *>(out);
@@ -425,7 +447,8 @@ constexpr uint32_t SEG_EDGES = 512;
 constexpr uint32_t SEG_LONG = 256;
 constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
 constexpr uint32_t LONG_FLAG = 0x40000000u;    // exact piece of a long row
-constexpr uint32_t ROW_MASK = 0x3fffffffu;
+constexpr uint32_t CONST_FLAG = 0x20000000u;   // rows without in-edges
+constexpr uint32_t ROW_MASK = 0x1fffffffu;     // work-list variants take N < 2^29
 // Two block shapes: WIDE, one block of 32 warps per SM, and NARROW, blocks
 // of 8 warps, several per SM (more warps in flight, fewer registers).
 // Shared memory holds each warp's gather buffer and, after it, a cache of
@@ -441,15 +464,39 @@ constexpr int pull_min_blocks(int block, bool exact) { return block == PULL_WIDE
 constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
 constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
-__global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ counts)
+// Work-list construction.  Rows are first partitioned, stably, into the
+// rows with in-edges and the rows without (rows[0, ne) and rows[ne, N)):
+// short items are cut over the first part, so a warp's 32 rows all carry
+// edges, and the rows without in-edges become CONST items at the end of the
+// list -- for the div variants their rank and contribution are the same
+// from the second iteration on, so later iterations leave them out.
+__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ flag)
 {
-    // one thread per 32-row window: the long-row pieces it will emit
-    // (counts[w]) and its short-row items (counts[windows + w])
-    const uint64_t windows = (n + 31) / 32;
+    for (uint64_t r = gtid(); r < n; r += gthreads()) flag[r] = off[r + 1] > off[r] ? 1u : 0u;
+}
+
+__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, const uint32_t *__restrict__ pos,
+                                uint32_t *__restrict__ rows)
+{
+    const uint64_t ne = pos[n];
+    for (uint64_t r = gtid(); r < n; r += gthreads()) {
+        if (off[r + 1] > off[r]) rows[pos[r]] = static_cast<uint32_t>(r);
+        else rows[ne + (r - pos[r])] = static_cast<uint32_t>(r);
+    }
+}
+
+// One thread per window of 32 rows of rows[0, ne): the long-row pieces
+// (counts[w]) and short items (counts[W + w]) it emits; counts[2W + w]: the
+// CONST item of window w of rows[ne, N).
+__global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
+                            const uint32_t *__restrict__ pos, uint64_t n, uint32_t *__restrict__ counts)
+{
+    const uint64_t windows = (n + 31) / 32, ne = pos[n];
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
-        const uint64_t r0 = w * 32, r1 = min(n, r0 + 32);
+        const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
         uint32_t pieces = 0, items = 0, acc_edges = 0, acc_rows = 0;
-        for (uint64_t r = r0; r < r1; r++) {
+        for (uint64_t k = k0; k < k1; k++) {
+            const uint32_t r = rows[k];
             const uint32_t d = off[r + 1] - off[r];
             if (d > SEG_LONG) {
                 if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
@@ -462,41 +509,53 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, uint64_t n, uint32
         if (acc_rows) items++;
         counts[w] = pieces;
         counts[windows + w] = items;
+        counts[2 * windows + w] = w * 32 < n - ne ? 1u : 0u;
     }
 }
 
-__global__ void k_seg_emit(const uint32_t *__restrict__ off, uint64_t n, int split,
+// Items: pieces {row, row + 1 | PIECE or LONG, e0, e1}; short items
+// {k0, k1, e0, e1} over rows[k0, k1) (their edges are contiguous: rows in
+// between have none); CONST items {ne + k0, ne + k1 | CONST, 0, 0}.
+__global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
+                           const uint32_t *__restrict__ pos, uint64_t n, int split,
                            const uint32_t *__restrict__ first, uint4 *__restrict__ work,
                            uint32_t *__restrict__ long_count)
 {
-    const uint64_t windows = (n + 31) / 32;
+    const uint64_t windows = (n + 31) / 32, ne = pos[n];
     const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
-        const uint64_t r0 = w * 32, r1 = min(n, r0 + 32);
+        const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
         uint32_t piece_out = first[w], out = first[windows + w];
-        uint64_t start_row = r0;
+        uint64_t start = k0;
         uint32_t acc_edges = 0, acc_rows = 0;
-        for (uint64_t r = r0; r < r1; r++) {
+        for (uint64_t k = k0; k < k1; k++) {
+            const uint32_t r = rows[k];
             const uint32_t d = off[r + 1] - off[r];
             if (d > SEG_LONG) {
                 if (acc_rows) {
-                    work[out++] = make_uint4(uint32_t(start_row), uint32_t(r), off[start_row], off[r]);
+                    work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
                     acc_rows = 0; acc_edges = 0;
                 }
                 for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
-                    work[piece_out++] = make_uint4(uint32_t(r), uint32_t(r + 1) | flag, p,
-                                                   min(p + SEG_EDGES, off[r + 1]));
+                    work[piece_out++] = make_uint4(r, (r + 1) | flag, p, min(p + SEG_EDGES, off[r + 1]));
                 long_count[r] = 0;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) {
-                work[out++] = make_uint4(uint32_t(start_row), uint32_t(r), off[start_row], off[r]);
+                work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
                 acc_rows = 0; acc_edges = 0;
             }
-            if (acc_rows == 0) start_row = r;
+            if (acc_rows == 0) start = k;
             acc_rows++; acc_edges += d;
         }
-        if (acc_rows) work[out++] = make_uint4(uint32_t(start_row), uint32_t(r1), off[start_row], off[r1]);
+        if (acc_rows) {
+            const uint32_t last = rows[k1 - 1];
+            work[out++] = make_uint4(uint32_t(start), uint32_t(k1), off[rows[start]], off[last + 1]);
+        }
+        if (w * 32 < n - ne) {
+            const uint64_t c0 = ne + w * 32, c1 = min(n, c0 + 32);
+            work[first[2 * windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
+        }
     }
 }
 
@@ -666,6 +725,7 @@ template<bool NODIV, bool EXACT_LONG, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_pr_pull_items(PrArgs a)
 {
     constexpr int PULL_WARPS = BLOCK / 32;
+    resolve_args(a);
     extern __shared__ __align__(16) float smem_f[];
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
@@ -749,21 +809,27 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
             }
             continue;
         }
-        // up to 32 short rows: lane l owns row r0 + l; its row end and
+        // up to 32 rows rows[r0 + l]: lane l owns one; its row end and
         // consolidation inputs are loaded alongside the gathers
         const uint32_t rows = r1 - r0, len = e1 - e0;
+        uint32_t row = 0;
         FinishIn fin{0.0f, 0u, 0u};
         if (lane < rows) {
-            s_end[lane] = a.rev_v[r0 + lane + 1] - e0;
-            fin = finish_load<NODIV>(a, r0 + lane);
+            row = a.rows[r0 + lane];
+            fin = finish_load<NODIV>(a, row);
         }
+        if (w.y & CONST_FLAG) {                            // no in-edges: the sum is +0
+            if (lane < rows) dsum += finish_store<NODIV>(a, row, 0.0f, base_nd, fin);
+            continue;
+        }
+        if (lane < rows) s_end[lane] = a.rev_v[row + 1] - e0;
         gather_into(ge, src, hub, hubs, e0, len, buf, lane);
         __syncwarp();
         if (lane < rows) {
             const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
             float sum = 0.0f;
             for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
-            dsum += finish_store<NODIV>(a, r0 + lane, sum, base_nd, fin);
+            dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
         }
         __syncwarp();
     }
@@ -799,6 +865,9 @@ struct PrRun {
     uint32_t *long_count = nullptr;
     uint32_t *win_counts = nullptr;
     float *vals = nullptr;             // exact long rows: gathered terms (edge-indexed)
+    uint32_t *rows = nullptr;          // rows with in-edges, then rows without
+    const uint32_t *count_all = nullptr;       // device: items in the list
+    const uint32_t *count_nonconst = nullptr;  // device: items before the CONST ones
 };
 
 struct Geometry { unsigned block, grid; size_t smem; };
@@ -887,34 +956,44 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
 int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &run, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count;
+    if (n > ROW_MASK) return BW_ERR_TOO_LARGE;
     const uint64_t windows = (n + 31) / 32;
-    // Row groups <= N; pieces <= M / SEG_EDGES + (rows longer than
-    // SEG_LONG) <= M / SEG_EDGES + M / SEG_LONG.
-    const uint64_t cap = windows + n + g->edge_count / SEG_EDGES + g->edge_count / SEG_LONG + 16;
-    // counts: [pieces of window 0..W-1 | short items of window 0..W-1 | 0],
-    // scanned in place into first positions (the last entry: the total)
-    const uint64_t entries = 2 * windows + 1;
-    size_t temp = 0;
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp, static_cast<uint32_t *>(nullptr),
+    // Short items <= N + W; pieces <= M / SEG_EDGES + M / SEG_LONG; CONST <= W.
+    const uint64_t cap = 2 * windows + n + g->edge_count / SEG_EDGES + g->edge_count / SEG_LONG + 16;
+    // scan areas: row flags (N + 1) -> positions; window counts
+    // [pieces | short items | const items | 0] (3W + 1) -> first positions
+    const uint64_t entries = 3 * windows + 1;
+    size_t temp_rows = 0, temp_items = 0;
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp_rows, static_cast<uint32_t *>(nullptr),
+                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(n + 1), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp_items, static_cast<uint32_t *>(nullptr),
                                           static_cast<uint32_t *>(nullptr), static_cast<int64_t>(entries), s));
-    const uint64_t temp_at = (2 * entries + 63) & ~uint64_t(63);   // 256-byte aligned scan storage
-    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.win_counts), temp_at * sizeof(uint32_t) + temp, s));
+    auto align64 = [](uint64_t words) { return (words + 63) & ~uint64_t(63); };   // 256-byte boundaries
+    const uint64_t at_pos = align64(n + 1), at_counts = at_pos + align64(n + 1),
+                   at_first = at_counts + align64(entries), at_temp = at_first + align64(entries);
+    const size_t temp = std::max(temp_rows, temp_items);
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.win_counts), at_temp * sizeof(uint32_t) + temp, s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
-    uint32_t *counts = run.win_counts + entries;
-    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, counts);
-    BW_CUDA(cudaMemsetAsync(counts + 2 * windows, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(run.win_counts + temp_at, temp, counts, run.win_counts,
-                                          static_cast<int64_t>(entries), s));
-    k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, split, run.win_counts, run.work, run.long_count);
-    ctx->launches += 2;                  // k_seg_count, k_seg_emit (the scan is the library's)
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.rows), n * sizeof(uint32_t), s));
+    uint32_t *flags = run.win_counts, *pos = run.win_counts + at_pos;
+    uint32_t *counts = run.win_counts + at_counts, *first = run.win_counts + at_first;
+    void *scratch = run.win_counts + at_temp;
+    k_row_flags<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, flags);
+    BW_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(scratch, temp_rows, flags, pos, static_cast<int64_t>(n + 1), s));
+    k_row_partition<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, pos, run.rows);
+    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, counts);
+    BW_CUDA(cudaMemsetAsync(counts + 3 * windows, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(scratch, temp_items, counts, first, static_cast<int64_t>(entries), s));
+    k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, split, first, run.work,
+                                                  run.long_count);
+    ctx->launches += 4;                  // flags, partition, count, emit (the scans are the library's)
     BW_CUDA(cudaGetLastError());
-    uint32_t totals[2] = {0, 0};       // pieces (the exclusive prefix at W), all items
-    BW_CUDA(cudaMemcpyAsync(&totals[0], run.win_counts + windows, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    BW_CUDA(cudaMemcpyAsync(&totals[1], run.win_counts + 2 * windows, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    BW_CUDA(cudaStreamSynchronize(s));
-    run.work_count = totals[1];
-    if (!split && totals[0])
+    // the list's length stays on the device (no host round trip in a run)
+    run.count_all = first + 3 * windows;
+    run.count_nonconst = first + 2 * windows;
+    if (!split && g->edge_count)
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), g->edge_count * sizeof(float), s));
     return BW_OK;
 }
@@ -925,7 +1004,8 @@ void free_run(PrRun &run, cudaStream_t s)
     if (run.long_count) cudaFreeAsync(run.long_count, s);
     if (run.win_counts) cudaFreeAsync(run.win_counts, s);
     if (run.vals) cudaFreeAsync(run.vals, s);
-    run.work = nullptr; run.long_count = nullptr; run.win_counts = nullptr; run.vals = nullptr;
+    if (run.rows) cudaFreeAsync(run.rows, s);
+    run.work = nullptr; run.long_count = nullptr; run.win_counts = nullptr; run.vals = nullptr; run.rows = nullptr;
 }
 
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
@@ -966,46 +1046,43 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
 struct Relabel {
     uint32_t *slot = nullptr;     // vertex -> position in the gathered array
     uint32_t *gat_e = nullptr;    // reverse-CSR sources as positions
+    uint32_t *on = nullptr;       // device: the order was taken
     void *scratch = nullptr;
 };
 
 // Orders vertices by decreasing out-degree class (floor(log2(deg))), stable
 // in vertex order, and translates the reverse CSR's sources (one pass over
-// M).  Runs after the degrees, inside the timed region.  Unless `force`,
-// it stops after the (cheap) ordering when the first `hubs` entries would
-// cover less than 5% more of the edges than in vertex order; `used` tells.
+// M).  Runs after the degrees, inside the timed region.  Unless `force`, a
+// one-block kernel decides on the device whether the first `hubs` entries
+// would cover at least 5% more of the edges than in vertex order; the slot
+// and translation kernels, and every iteration, read that decision.
 int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, uint32_t hubs, bool force,
-                  Relabel &r, bool &used, cudaStream_t s)
+                  Relabel &r, cudaStream_t s)
 {
-    used = false;
     const uint64_t n = g->vertex_count, m = g->edge_count;
     size_t temp = 0;
     cub::DoubleBuffer<uint32_t> keys(nullptr, nullptr), ids(nullptr, nullptr);
     BW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
     const size_t words = 4 * n, temp_words = (temp + 3) / 4;
-    const size_t cov_at = (words + temp_words + 1) & ~size_t(1);       // two 64-bit counters after the sort
-    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (cov_at + 4) * sizeof(uint32_t), s));
+    const size_t on_at = words + temp_words;
+    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (on_at + 1) * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
     uint32_t *base = static_cast<uint32_t *>(r.scratch);
+    r.on = base + on_at;
     keys = cub::DoubleBuffer<uint32_t>(base, base + n);
     ids = cub::DoubleBuffer<uint32_t>(base + 2 * n, base + 3 * n);
     k_relabel_keys<<<ctx->sm_count * 4, 256, 0, s>>>(deg, n, keys.Current(), ids.Current());
     ctx->launches++;
     BW_CUDA(cub::DeviceRadixSort::SortPairs(base + words, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
-    if (!force) {
-        unsigned long long *cov = reinterpret_cast<unsigned long long *>(base + cov_at);
-        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, ids.Current(), std::min<uint64_t>(hubs, n), cov);
+    if (force) {
+        BW_CUDA(cudaMemsetAsync(r.on, 1, sizeof(uint32_t), s));
+    } else {
+        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, ids.Current(), std::min<uint64_t>(hubs, n), m, r.on);
         ctx->launches++;
-        unsigned long long host_cov[2] = {0, 0};
-        BW_CUDA(cudaMemcpyAsync(host_cov, cov, sizeof host_cov, cudaMemcpyDeviceToHost, s));
-        BW_CUDA(cudaStreamSynchronize(s));
-        if (static_cast<double>(host_cov[0]) - static_cast<double>(host_cov[1]) < 0.05 * static_cast<double>(m))
-            return BW_OK;
     }
-    used = true;
-    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.slot);
-    if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.slot, r.gat_e);
+    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.on, r.slot);
+    if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.on, r.slot, r.gat_e);
     ctx->launches += m ? 2 : 1;
     BW_CUDA(cudaGetLastError());
     return BW_OK;
@@ -1103,20 +1180,20 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     Relabel rl;
     const uint32_t flags = cfg ? cfg->flags : 0u;
     const bool force = (flags & BW_LAUNCH_RELABEL) != 0;
-    bool relabel = false;
+    bool relabel = false;                 // may be taken (the device decides)
     if (all_items && g->edge_count > 0 && !(flags & BW_LAUNCH_NO_RELABEL) &&
         (force || (iterations >= 4 && a.hub_count > 0))) {
-        const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, relabel, s);
+        const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, s);
         if (rc != BW_OK) {
             free_relabel(rl, s);
             free_run(split_run, s);
             free_run(exact_run, s);
             return rc;
         }
-        if (relabel) {
-            a.slot = rl.slot;
-            a.gat_e = rl.gat_e;
-        }
+        relabel = true;
+        a.slot = rl.slot;
+        a.gat_e = rl.gat_e;
+        a.relabel_on = rl.on;
     }
     // nodiv + relabelled sources: the gathered copy of the ranks, in slot order
     float *gat[2] = {ctx->pr_buf[1], ctx->pr_acc};
@@ -1162,9 +1239,12 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         }
         const PrRun &items = v == PR_PULL_SEGMENTED ? split_run : exact_run;
         a.work = items.work;
-        a.work_count = items.work_count;
         a.long_count = items.long_count;
         a.vals = items.vals;
+        a.rows = items.rows;
+        // div: rows without in-edges hold the same rank and contribution in
+        // both buffers once iterations 1 and 2 have written them
+        a.count_dev = items.work ? ((!nodiv && j > 2) ? items.count_nonconst : items.count_all) : nullptr;
         Geometry geo = geometry(ctx, v, cfg);
         BW_TRY(launch_iteration(ctx, v, a, geo, s));
         (void) loop_mode;

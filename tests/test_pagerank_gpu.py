@@ -148,12 +148,14 @@ def test_diffs_reported(ctx, graphs):
 
 def test_kernel_launch_count(ctx, graphs, long_graphs):
     """The run reports exactly the kernels of this library it launched:
-    degrees (row lengths), work list (count + emit), the relabel decision
-    (keys + coverage, then slots + edges when taken), init, one kernel per
-    fused iteration or two (scatter + consolidation) otherwise."""
-    _, g = graphs["rmat14"]                     # hub cache holds every vertex: no relabel
-    assert bw.pagerank(ctx, g, "vertex-pull", 5).kernel_launches == 1 + 2 + 2 + 1 + 5
-    assert bw.pagerank(ctx, g, "vertex-pull", 2).kernel_launches == 1 + 2 + 1 + 2
+    degrees (row lengths), work list (row flags, partition, count, emit),
+    the hub-first order (keys, the device-side decision unless forced,
+    slots, source translation -- the last two return at once when the
+    order is not taken), init, one kernel per fused iteration or two
+    (scatter + consolidation) otherwise."""
+    _, g = graphs["rmat14"]
+    assert bw.pagerank(ctx, g, "vertex-pull", 5).kernel_launches == 1 + 4 + 4 + 1 + 5
+    assert bw.pagerank(ctx, g, "vertex-pull", 2).kernel_launches == 1 + 4 + 1 + 2
     assert bw.pagerank(ctx, g, "rev-edge-list", 5).kernel_launches == 1 + 1 + 2 * 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 2 + 3 + 1 + 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 2 + 1 + 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 4 + 3 + 1 + 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 4 + 1 + 5
