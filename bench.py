@@ -50,6 +50,23 @@ def _dist():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(value: float, ws: int, device="cpu") -> float:
+    """The slowest rank's value (timings are reported as the max over ranks)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ws: int, edges: int, iterations: int, seconds: float) -> float:
+    """Whole-job GTEPS of `ws` independent replicas that each ran
+    `iterations` PageRank iterations over `edges` edges in `seconds`."""
+    return ws * edges * iterations / seconds / 1e9
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -319,13 +336,9 @@ def run_ours(args):
         torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
-    ms = t0.elapsed_time(t1)
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(t0.elapsed_time(t1), ws, device=f"cuda:{dev}")
     ms_per_step = ms / args.steps
-    value = ws * m * ITERATIONS / (ms_per_step * 1e-3) / 1e9
+    value = replica_throughput(ws, m, ITERATIONS, ms_per_step * 1e-3)
 
     kernel_ms = float(np.median(iter_ms))
     ab = alg_bytes(variant, n, m)
@@ -348,12 +361,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t)
-    e2e_s = float(np.mean(e2e_times))
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * m * ITERATIONS / e2e_s / 1e9
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), ws, device=f"cuda:{dev}")
+    e2e_value = replica_throughput(ws, m, ITERATIONS, e2e_s)
     h2d = e2e.h2d_bytes
     del g, e2e
     torch.cuda.empty_cache()

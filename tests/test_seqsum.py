@@ -33,7 +33,8 @@ static uint32_t sequential(const std::vector<float> &x) {
 }
 
 // Terms added in order by one lane before the map scan takes over (the
-// kernel's SERIAL_TERMS); the checker runs with 0 and with 1024.
+// kernel's SERIAL_TERMS); the checker runs several values, including ones
+// that end inside a window.
 static uint32_t serial_terms = 0;
 
 // Warp emulation; returns false when the kernel would fall back.
@@ -41,11 +42,13 @@ static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
     const uint32_t L = 8, WIN = 32 * L, n = vals.size();
     uint32_t sb = 0;
     for (uint32_t w = 0; w < n; w += WIN) {
-        if (w < serial_terms) {
+        uint32_t pos = 0;
+        if (w < serial_terms) {            // terms [w, serial_terms) in order by one lane
             volatile float acc = bf(sb);
-            for (uint32_t i = w; i < n && i < w + WIN; i++) acc = acc + vals[i];
+            uint32_t i = w;
+            for (; i < n && i < w + WIN && i < serial_terms; i++) acc = acc + vals[i];
             sb = fb(acc);
-            continue;
+            pos = i - w;
         }
         uint32_t x[32][8];
         for (uint32_t lane = 0; lane < 32; lane++)
@@ -54,7 +57,6 @@ static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
                 x[lane][u] = w + k < n ? fb(vals[w + k]) : 0u;
             }
         const uint32_t lim = n - w < WIN ? n - w : WIN;
-        uint32_t pos = 0;
         int guard = 0;
         while (pos < lim) {
             if (++guard > 1000) return false;
@@ -148,7 +150,7 @@ static void check(const std::vector<float> &x, bool expect_domain) {
 static void run_all();
 
 int main() {
-    for (uint32_t st : {0u, 1024u}) { serial_terms = st; run_all(); }
+    for (uint32_t st : {0u, 64u, 300u, 1024u}) { serial_terms = st; run_all(); }
     std::printf("tested %d fallback %d bad %d\n", tested, fallback, bad);
     return bad ? 1 : 0;
 }
