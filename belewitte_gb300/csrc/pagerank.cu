@@ -153,6 +153,39 @@ __global__ void __launch_bounds__(256) k_count_ids(const uint32_t *__restrict__ 
     }
 }
 
+// The same histogram for a stream whose hot ids are low (R-MAT and
+// preferential-attachment graphs number their hubs first): ids below
+// COUNT_PRIVATE are counted in the block's shared memory and added to the
+// global counts once per block; the rest as in k_count_ids.  Thousands of
+// atomics on one hub's counter otherwise serialise at its L2 slice.
+constexpr uint32_t COUNT_PRIVATE = 8192;
+
+__global__ void __launch_bounds__(1024) k_count_ids_private(const uint32_t *__restrict__ ids, uint64_t count,
+                                                            uint32_t stride_words, uint64_t n,
+                                                            uint32_t *__restrict__ deg)
+{
+    __shared__ uint32_t local[COUNT_PRIVATE];
+    const uint32_t priv = static_cast<uint32_t>(n < COUNT_PRIVATE ? n : COUNT_PRIVATE);
+    for (uint32_t i = threadIdx.x; i < priv; i += blockDim.x) local[i] = 0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    for (uint64_t base = warp * 32; base < count; base += warps * 32) {
+        const uint64_t i = base + lane;
+        const uint32_t id = i < count ? ids[i * stride_words] : 0xffffffffu;
+        if (id < priv) {
+            atomicAdd(&local[id], 1u);
+        } else {
+            const unsigned peers = __match_any_sync(__activemask(), id);
+            if (id != 0xffffffffu && (__ffs(peers) - 1) == static_cast<int>(lane))
+                atomicAdd(&deg[id], static_cast<uint32_t>(__popc(peers)));
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < priv; i += blockDim.x)
+        if (local[i]) atomicAdd(&deg[i], local[i]);
+}
+
 // Initial ranks 1/N (pagerank/pagerank.cpp:88) and contributions (stored at
 // the vertex's slot when sources are relabelled; `gat` is the nodiv family's
 // relabelled copy of the ranks).
@@ -946,7 +979,9 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
       case PR_REV_STRUCT_EDGE_LIST:// reverseStructEdgeListComputeDegrees: edges[].out
         k_count_ids<<<grid, 256, 0, s>>>(g->rev_struct_edges + 1, g->edge_count, 2, deg); break;
       default:                     // reverseCSRComputeDegrees
-        k_count_ids<<<grid, 256, 0, s>>>(g->rev_edges, g->edge_count, 1, deg); break;
+        k_count_ids_private<<<ctx->sm_count * 2, 1024, 0, s>>>(g->rev_edges, g->edge_count, 1,
+                                                               g->vertex_count, deg);
+        break;
     }
     ctx->launches++;
     BW_CUDA(cudaGetLastError());

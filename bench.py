@@ -144,7 +144,7 @@ def _measured_peak():
 
 
 # The PageRank variant the headline is measured with: the fastest on this
-# workload in the on-device sweep of every variant (pull-segmented ~285 us,
+# workload in the on-device sweep of every variant (pull-segmented ~249 us,
 # rev-edge-list ~293 us, vertex-pull ~1.2 ms per iteration on R-MAT-22);
 # --variant measures another one.
 HEADLINE_VARIANT = "pull-segmented"
@@ -155,10 +155,14 @@ DOMINANT = {"pull-segmented": "k_pr_pull_items", "vertex-pull": "k_pr_pull_items
 
 
 def alg_bytes(variant: str, n: int, m: int) -> int:
-    """Compulsory bytes of one PageRank iteration."""
+    """Compulsory bytes of one PageRank iteration of the reference algorithm:
+    the edge stream (pull: 4M source indices; edge lists: 8M pairs), the
+    offsets (4(N+1), pull only), one read of the gathered vector (4N), the
+    degrees (4N), the previous ranks the diff compares with (4N) and the
+    rank writes (4N)."""
     if variant.startswith(("edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list")):
-        return 8 * m + 12 * n
-    return 4 * m + 16 * n + 4
+        return 8 * m + 16 * n
+    return 4 * m + 20 * n + 4
 
 
 def bfs_learned_vs_fixed(ctx, dev):
