@@ -90,6 +90,25 @@ BWS_HD bool step(uint32_t xb, uint32_t k, Map &m)
     return true;
 }
 
+// The same map without branches (selects only), for warps whose lanes take
+// different cases at once; `ok` is cleared for terms outside the domain.
+BWS_HD Map step_select(uint32_t xb, uint32_t k, bool &ok)
+{
+    const uint32_t kx = (xb >> 23) & 0xffu;
+    const bool zero = (xb & 0x7fffffffu) == 0;
+    ok = ok && (zero || !((xb >> 31) || kx == 0 || kx == 0xffu));
+    const int32_t d = static_cast<int32_t>(k) - static_cast<int32_t>(kx);
+    const uint32_t dd = static_cast<uint32_t>(d < 1 ? 1 : (d > 24 ? 24 : d));
+    const uint32_t mx = (xb & 0x7fffffu) | ONE;
+    const uint32_t q = mx >> dd, rem = mx & ((1u << dd) - 1u), half = 1u << (dd - 1u);
+    const uint32_t up = rem > half ? 1u : 0u, tie = rem == half ? 1u : 0u, odd = q & 1u;
+    uint32_t e = q + (up | (tie & odd)), o = q + (up | (tie & (odd ^ 1u)));
+    const bool big = d <= 0, tiny = d >= 25 || zero;
+    e = big ? SAT : (tiny ? 0u : e);
+    o = big ? SAT : (tiny ? 0u : o);
+    return Map{e, o};
+}
+
 BWS_HD uint32_t exponent_of(uint32_t sb) { return (sb >> 23) & 0xffu; }
 BWS_HD uint32_t significand_of(uint32_t sb) { return (sb & 0x7fffffu) | ONE; }
 BWS_HD uint32_t bits_of(uint32_t k, uint32_t a) { return (k << 23) | (a & 0x7fffffu); }

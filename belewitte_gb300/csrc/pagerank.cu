@@ -84,6 +84,10 @@ struct PrArgs {
     const uint32_t *slot;
     uint32_t hub_count;        // work-list kernels: gathered entries cached in shared memory
     const uint32_t *rows;      // work-list kernels: rows with in-edges, then rows without
+    const uint32_t *long_rows;    // exact variants: long rows by decreasing length
+    const uint32_t *long_total;   // device: number of long rows
+    const uint32_t *giant_total;  // device: long rows summed by a whole warp (the first ones)
+    uint32_t *sum_ctr;            // k_pr_long_sums' job and finish counters
     // Decided on the device, so the host never waits inside a run:
     const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
@@ -467,15 +471,14 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
 // sequential summation (pagerank/vertex_pull.cu:23-27), so these rows are
 // bit-identical to it.
 // Long rows (more than SEG_LONG edges) are cut into SEG_EDGES-edge pieces
-// that any warp takes; the work list puts every piece before the short-row
-// items so that long rows finish early.  The last piece of a row to arrive
-// (arrival counter) completes it:
+// that any warp takes; the work list puts every piece, longest rows first,
+// before the short-row items:
 //   EXACT (vertex-pull, vertex-pull-nodiv): pieces store their gathered
-//   terms in vals[] (edge order); the last one evaluates the row's
-//   sequential sum with the whole warp (warp_sequential_sum, bit-identical
-//   to the reference's loop) and consolidates the vertex.
+//   terms in vals[] (edge order); k_pr_long_sums then evaluates every long
+//   row's sequential sum (bit-identical to the reference's loop) and
+//   consolidates it.
 //   split (pull-segmented): pieces add lane partials (shuffle tree) into
-//   acc[] with float atomics; the last one consolidates the row.
+//   acc[] with float atomics; the last piece of the row consolidates it.
 constexpr uint32_t SEG_EDGES = 512;
 constexpr uint32_t SEG_LONG = 256;
 constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
@@ -497,68 +500,123 @@ constexpr int pull_min_blocks(int block, bool exact) { return block == PULL_WIDE
 constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
 constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
-// Work-list construction.  Rows are first partitioned, stably, into the
-// rows with in-edges and the rows without (rows[0, ne) and rows[ne, N)):
-// short items are cut over the first part, so a warp's 32 rows all carry
-// edges, and the rows without in-edges become CONST items at the end of the
-// list -- for the div variants their rank and contribution are the same
-// from the second iteration on, so later iterations leave them out.
-__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ flag)
+// Work-list construction.
+//  * Rows are partitioned, stably, into the rows with in-edges and the rows
+//    without (rows[0, ne) and rows[ne, N)).  Short items are cut over the
+//    first part, so a warp's 32 rows all carry edges; the rows without
+//    in-edges become CONST items at the end of the list (for the div
+//    variants their rank and contribution are the same from the second
+//    iteration on, so later iterations leave them out).
+//  * Long rows (more than SEG_LONG edges) are sorted by decreasing length
+//    and cut into SEG_EDGES pieces in that order, at the front of the list.
+// Layout: [pieces | short items | CONST items]; the lengths stay on the
+// device (tot[0] = items before the CONST ones, tot[1] = all items).
+__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ flag,
+                            uint32_t *__restrict__ long_flag)
 {
-    for (uint64_t r = gtid(); r < n; r += gthreads()) flag[r] = off[r + 1] > off[r] ? 1u : 0u;
-}
-
-__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, const uint32_t *__restrict__ pos,
-                                uint32_t *__restrict__ rows)
-{
-    const uint64_t ne = pos[n];
     for (uint64_t r = gtid(); r < n; r += gthreads()) {
-        if (off[r + 1] > off[r]) rows[pos[r]] = static_cast<uint32_t>(r);
-        else rows[ne + (r - pos[r])] = static_cast<uint32_t>(r);
+        const uint32_t d = off[r + 1] - off[r];
+        flag[r] = d ? 1u : 0u;
+        long_flag[r] = d > SEG_LONG ? 1u : 0u;
     }
 }
 
-// One thread per window of 32 rows of rows[0, ne): the long-row pieces
-// (counts[w]) and short items (counts[W + w]) it emits; counts[2W + w]: the
-// CONST item of window w of rows[ne, N).
+__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, const uint32_t *__restrict__ pos,
+                                const uint32_t *__restrict__ long_pos, uint32_t *__restrict__ rows,
+                                uint32_t *__restrict__ long_len, uint32_t *__restrict__ long_row)
+{
+    const uint64_t ne = pos[n];
+    for (uint64_t r = gtid(); r < n; r += gthreads()) {
+        const uint32_t d = off[r + 1] - off[r];
+        if (d) rows[pos[r]] = static_cast<uint32_t>(r);
+        else rows[ne + (r - pos[r])] = static_cast<uint32_t>(r);
+        if (d > SEG_LONG) {
+            long_len[long_pos[r]] = d;
+            long_row[long_pos[r]] = static_cast<uint32_t>(r);
+        }
+    }
+}
+
+// Piece counts of the sorted long rows (0 past the last one).
+__global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
+                              uint64_t cap, uint32_t *__restrict__ pieces)
+{
+    const uint64_t L = *long_total;
+    for (uint64_t i = gtid(); i < cap; i += gthreads())
+        pieces[i] = i < L ? (long_len[i] + SEG_EDGES - 1) / SEG_EDGES : 0u;
+}
+
+// Exact long rows above GIANT_ROW terms are summed by a whole warp (binade
+// maps over coalesced windows); shorter ones in batches of 32, one row per
+// lane.
+constexpr uint32_t GIANT_ROW = 4096;
+
+// Pieces of sorted long row i at [ppos[i], ppos[i + 1]); the split
+// variant's arrival counters cleared; the number of rows above GIANT_ROW.
+__global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ long_row,
+                             const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
+                             const uint32_t *__restrict__ ppos, int split, uint4 *__restrict__ work,
+                             uint32_t *__restrict__ long_count, uint32_t *__restrict__ giant_total)
+{
+    const uint64_t L = *long_total;
+    uint64_t lo = 0, hi = L;                       // giant rows come first (lengths decrease)
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if (long_len[mid] > GIANT_ROW) lo = mid + 1; else hi = mid;
+    }
+    if (gtid() == 0) *giant_total = static_cast<uint32_t>(lo);
+    const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
+    for (uint64_t i = gtid(); i < L; i += gthreads()) {
+        const uint32_t r = long_row[i];
+        uint32_t out = ppos[i];
+        for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
+            work[out++] = make_uint4(r, (r + 1) | flag, p, min(p + SEG_EDGES, off[r + 1]));
+        long_count[r] = 0;
+    }
+}
+
+// One thread per window of 32 rows of rows[0, ne): the short items it emits
+// (counts[w]); counts[W + w]: the CONST item of window w of rows[ne, N).
 __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
                             const uint32_t *__restrict__ pos, uint64_t n, uint32_t *__restrict__ counts)
 {
     const uint64_t windows = (n + 31) / 32, ne = pos[n];
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
         const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
-        uint32_t pieces = 0, items = 0, acc_edges = 0, acc_rows = 0;
+        uint32_t items = 0, acc_edges = 0, acc_rows = 0;
         for (uint64_t k = k0; k < k1; k++) {
             const uint32_t r = rows[k];
             const uint32_t d = off[r + 1] - off[r];
-            if (d > SEG_LONG) {
+            if (d > SEG_LONG) {                 // long rows go to pieces
                 if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
-                pieces += (d + SEG_EDGES - 1) / SEG_EDGES;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) { items++; acc_rows = 0; acc_edges = 0; }
             acc_rows++; acc_edges += d;
         }
         if (acc_rows) items++;
-        counts[w] = pieces;
-        counts[windows + w] = items;
-        counts[2 * windows + w] = w * 32 < n - ne ? 1u : 0u;
+        counts[w] = items;
+        counts[windows + w] = w * 32 < n - ne ? 1u : 0u;
     }
 }
 
-// Items: pieces {row, row + 1 | PIECE or LONG, e0, e1}; short items
-// {k0, k1, e0, e1} over rows[k0, k1) (their edges are contiguous: rows in
-// between have none); CONST items {ne + k0, ne + k1 | CONST, 0, 0}.
+// Short items {k0, k1, e0, e1} over rows[k0, k1) (their edges are
+// contiguous: rows in between have none); CONST items
+// {ne + k0, ne + k1 | CONST, 0, 0}; both after the P pieces.
 __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                           const uint32_t *__restrict__ pos, uint64_t n, int split,
-                           const uint32_t *__restrict__ first, uint4 *__restrict__ work,
-                           uint32_t *__restrict__ long_count)
+                           const uint32_t *__restrict__ pos, uint64_t n, const uint32_t *__restrict__ first,
+                           const uint32_t *__restrict__ piece_total, uint4 *__restrict__ work,
+                           uint32_t *__restrict__ tot)
 {
     const uint64_t windows = (n + 31) / 32, ne = pos[n];
-    const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
+    const uint32_t P = *piece_total;
+    if (gtid() == 0) {
+        tot[0] = P + first[windows];
+        tot[1] = P + first[2 * windows];
+    }
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
         const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
-        uint32_t piece_out = first[w], out = first[windows + w];
+        uint32_t out = P + first[w];
         uint64_t start = k0;
         uint32_t acc_edges = 0, acc_rows = 0;
         for (uint64_t k = k0; k < k1; k++) {
@@ -569,9 +627,6 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
                     work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
                     acc_rows = 0; acc_edges = 0;
                 }
-                for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
-                    work[piece_out++] = make_uint4(r, (r + 1) | flag, p, min(p + SEG_EDGES, off[r + 1]));
-                long_count[r] = 0;
                 continue;
             }
             if (acc_rows && acc_edges + d > SEG_EDGES) {
@@ -587,11 +642,50 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
         }
         if (w * 32 < n - ne) {
             const uint64_t c0 = ne + w * 32, c1 = min(n, c0 + 32);
-            work[first[2 * windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
+            work[P + first[windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
         }
     }
 }
 
+// One lane's sequential float sum of p[0, len) -- the reference's row loop.
+// Four-term vector loads once aligned; the next 32 terms are in flight
+// while the current 32 are added (the data were written by the previous
+// kernel).
+__device__ __forceinline__ float lane_sequential_sum(const float *p, uint32_t len)
+{
+    constexpr uint32_t Q = 8;                     // quads per stage
+    float acc = 0.0f;
+    uint32_t i = 0;
+    while (i < len && (reinterpret_cast<uintptr_t>(p + i) & 15)) acc = __fadd_rn(acc, __ldcg(p + i++));
+    const float4 *q = reinterpret_cast<const float4 *>(p + i);
+    const uint32_t quads = (len - i) / 4;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 cur[Q];
+#pragma unroll
+    for (uint32_t u = 0; u < Q; u++) cur[u] = u < quads ? __ldcg(q + u) : zero;
+    uint32_t k = 0;
+    for (; k + Q <= quads; k += Q) {
+        float4 nxt[Q];
+#pragma unroll
+        for (uint32_t u = 0; u < Q; u++) nxt[u] = k + Q + u < quads ? __ldcg(q + k + Q + u) : zero;
+#pragma unroll
+        for (uint32_t u = 0; u < Q; u++) {
+            acc = __fadd_rn(acc, cur[u].x); acc = __fadd_rn(acc, cur[u].y);
+            acc = __fadd_rn(acc, cur[u].z); acc = __fadd_rn(acc, cur[u].w);
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < Q; u++) cur[u] = nxt[u];
+    }
+#pragma unroll
+    for (uint32_t u = 0; u + 1 < Q; u++) {        // the last 0-7 whole quads are in cur[]
+        if (k + u < quads) {
+            acc = __fadd_rn(acc, cur[u].x); acc = __fadd_rn(acc, cur[u].y);
+            acc = __fadd_rn(acc, cur[u].z); acc = __fadd_rn(acc, cur[u].w);
+        }
+    }
+    for (i += quads * 4; i < len; i++) acc = __fadd_rn(acc, __ldcg(p + i));
+    return acc;
+}
 
 // One gathered value: from the shared-memory hub cache when the source is
 // among the first `hubs` entries, else from global memory.
@@ -627,20 +721,25 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
 }
 
 // The sequential sum s = fl(s + vals[i]), i = 0..n-1, starting from +0 --
-// bit-identical to one thread's loop -- evaluated window by window (256
-// terms, staged in shared memory).  The first SERIAL_TERMS terms are added
-// by lane 0 in order: there the sum doubles every few terms, and a binade
-// crossing costs the map scan a restart.  The rest uses the binade maps of
-// bw_seqsum.h: 8 consecutive terms per lane, a scan of the lanes' maps, and
-// one float addition by the lane that holds the next binade crossing.
-// `stage` holds 264 floats of shared memory; `vals` was written in this
-// launch, so it is read through L2.  Every lane returns the sum.
+// bit-identical to one thread's loop -- evaluated window by window
+// (32 x L terms, staged in shared memory, the next window's loads in
+// flight).  The first SERIAL_TERMS terms are added by lane 0 in order:
+// there the sum doubles every few terms, and a binade crossing costs the
+// map scan a restart.  The rest uses the binade maps of bw_seqsum.h: each
+// lane composes the maps of its L consecutive terms as a tree (depth
+// log2 L, branch-free steps), the warp scans the lanes' maps, and the lane
+// that holds the next binade crossing adds that term with one float
+// addition.  `stage` holds 33 x L floats of shared memory per warp; `vals`
+// was written by the previous kernel, so it is read through L2.  Every lane
+// returns the sum.
 constexpr uint32_t SERIAL_TERMS = 1024;   // measured: 64 was 23% slower on R-MAT-22
 
+template<uint32_t L>
 __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t n, float *stage, unsigned lane)
 {
     using namespace bwseq;
-    constexpr uint32_t L = 8, WIN = 32 * L;
+    static_assert((L & (L - 1)) == 0 && L <= 32, "L: a power of two up to 32");
+    constexpr uint32_t WIN = 32 * L;
     uint32_t sb = 0;                       // bits of the running sum (warp-uniform)
     bool ok = true;
     float pre[L];
@@ -648,7 +747,7 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
     for (uint32_t u = 0; u < L; u++) pre[u] = u * 32 + lane < n ? __ldcg(vals + u * 32 + lane) : 0.0f;
     for (uint32_t w = 0; w < n && ok; w += WIN) {
         // window [w, w + WIN): coalesced loads, staged so that lane l reads
-        // terms 8l..8l+7 (element k at k + k / 32: no bank conflicts)
+        // terms l*L .. l*L + L-1 (element k at k + k / 32: no bank conflicts)
 #pragma unroll
         for (uint32_t u = 0; u < L; u++) stage[u * 33 + lane] = pre[u];
         __syncwarp();
@@ -658,7 +757,6 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
             const uint32_t k = lane * L + u;
             x[u] = __float_as_uint(stage[k + (k >> 5)]);
         }
-        __syncwarp();
         const uint32_t nw = w + WIN;
 #pragma unroll
         for (uint32_t u = 0; u < L; u++)
@@ -676,6 +774,7 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
             sb = __shfl_sync(FULL_MASK, bits, 0);
             pos = upto;
         }
+        __syncwarp();                      // stage is rewritten by the next window
         for (uint32_t guard = 0; pos < lim; guard++) {
             if (guard > WIN + 1) { ok = false; break; }
             if (sb == 0) {
@@ -694,17 +793,22 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
             }
             if (!in_domain(sb)) { ok = false; break; }
             const uint32_t K = exponent_of(sb), A = significand_of(sb);
-            Map m = identity();
-            bool bad = false;
+            // this lane's terms as maps (inactive terms: +0, the identity),
+            // composed as a tree
+            Map t[L];
+            bool good = true;
 #pragma unroll
             for (uint32_t u = 0; u < L; u++) {
-                if (first + u >= pos && first + u < lim) {
-                    Map t;
-                    bad |= !step(x[u], K, t);
-                    m = compose(m, t);
-                }
+                const bool live = first + u >= pos && first + u < lim;
+                t[u] = step_select(live ? x[u] : 0u, K, good);
             }
-            if (__any_sync(FULL_MASK, bad)) { ok = false; break; }
+#pragma unroll
+            for (uint32_t st = 1; st < L; st <<= 1) {
+#pragma unroll
+                for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
+            }
+            const Map m = t[0];
+            if (__any_sync(FULL_MASK, !good)) { ok = false; break; }
             Map incl = m;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -727,9 +831,9 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
 #pragma unroll
                 for (uint32_t u = 0; u < L; u++) {
                     if (np == 0 && first + u >= pos && first + u < lim) {
-                        Map t;
-                        step(x[u], K, t);
-                        const uint32_t b = apply(t, acc);
+                        Map tu;
+                        step(x[u], K, tu);
+                        const uint32_t b = apply(tu, acc);
                         if (b >= TOP) {
                             nb = __float_as_uint(__fadd_rn(__uint_as_float(bits_of(K, acc)), __uint_as_float(x[u])));
                             np = first + u + 1;
@@ -809,7 +913,8 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
             continue;
         }
         if (EXACT_LONG && (w.y & LONG_FLAG)) {
-            // exact piece: store the gathered terms, the last piece sums the row
+            // exact piece: store the gathered terms in edge order; the
+            // long-row sums run in k_pr_long_sums after this kernel
             const uint32_t len = e1 - e0;
             for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
                 uint32_t idx[GATHER_UNROLL];
@@ -822,22 +927,6 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
                 for (int u = 0; u < GATHER_UNROLL; u++) {
                     const uint32_t k = base + u * 32 + lane;
                     if (k < len) __stcg(a.vals + e0 + k, gather1(src, hub, hubs, idx[u]));
-                }
-            }
-            __threadfence();
-            __syncwarp();
-            const uint32_t row_begin = a.rev_v[r0], row_len = a.rev_v[r0 + 1] - row_begin;
-            uint32_t last = 0;
-            if (lane == 0) {
-                const uint32_t pieces = (row_len + SEG_EDGES - 1) / SEG_EDGES;
-                last = atomicAdd(&a.long_count[r0], 1u) + 1 == pieces;
-            }
-            if (__shfl_sync(FULL_MASK, last, 0)) {
-                __threadfence();
-                const float total = warp_sequential_sum(a.vals + row_begin, row_len, buf, lane);
-                if (lane == 0) {
-                    a.long_count[r0] = 0;
-                    dsum += finish_vertex<NODIV>(a, r0, total, base_nd);
                 }
             }
             continue;
@@ -869,6 +958,60 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
     add_diff(a.diff, dsum);
 }
 
+// Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
+// after the iteration's work-list kernel has stored every long row's terms
+// in vals[] (edge order).  Jobs are taken in order from a counter (no static
+// share, so a warp that drew a long job takes fewer): first the rows above
+// GIANT_ROW terms, longest first, each summed by one warp
+// (warp_sequential_sum); then batches of 32 shorter long rows of similar
+// length, one row per lane (lane_sequential_sum).  Every sum is the
+// reference's sequential loop, bit-identical.  The last warp to finish
+// resets the counters for the next iteration.
+constexpr int LONG_SUM_THREADS = 256;
+constexpr uint32_t TERMS_PER_LANE = 32;      // warp-sum windows of 1024 terms
+
+template<bool NODIV>
+__global__ void __launch_bounds__(LONG_SUM_THREADS) k_pr_long_sums(PrArgs a, uint32_t *ctr)
+{
+    __shared__ float stage[LONG_SUM_THREADS / 32][33 * TERMS_PER_LANE];
+    resolve_args(a);
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t L = *a.long_total, G = *a.giant_total;
+    const uint32_t jobs = G + (L - G + 31) / 32;
+    const float base_nd = nodiv_base(a.n);
+    float dsum = 0.0f;
+    for (;;) {
+        uint32_t job = 0;
+        if (lane == 0) job = atomicAdd(&ctr[0], 1u);
+        job = __shfl_sync(FULL_MASK, job, 0);
+        if (job >= jobs) break;
+        if (job < G) {
+            const uint32_t row = a.long_rows[job];
+            const uint32_t beg = a.rev_v[row], len = a.rev_v[row + 1] - beg;
+            const float total = warp_sequential_sum<TERMS_PER_LANE>(a.vals + beg, len, stage[wib], lane);
+            if (lane == 0) dsum += finish_vertex<NODIV>(a, row, total, base_nd);
+        } else {
+            const uint32_t k = G + (job - G) * 32 + lane;
+            if (k < L) {
+                const uint32_t row = a.long_rows[k];
+                const FinishIn fin = finish_load<NODIV>(a, row);
+                const uint32_t beg = a.rev_v[row];
+                const float sum = lane_sequential_sum(a.vals + beg, a.rev_v[row + 1] - beg);
+                dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
+            }
+        }
+    }
+    add_diff(a.diff, dsum);
+    // the last warp out resets the job counter
+    if (lane == 0) {
+        const uint32_t warps = gridDim.x * (blockDim.x / 32);
+        if (atomicAdd(&ctr[1], 1u) + 1 == warps) {
+            ctr[0] = 0;
+            ctr[1] = 0;
+        }
+    }
+}
+
 }  // namespace
 }  // namespace bw
 
@@ -892,13 +1035,15 @@ int check_reps(const bw_graph_view *g, int reps)
 
 // Per-run state of one PageRank execution.
 struct PrRun {
-    PrArgs a{};
     uint4 *work = nullptr;
-    uint32_t work_count = 0;
-    uint32_t *long_count = nullptr;
-    uint32_t *win_counts = nullptr;
+    uint32_t *long_count = nullptr;    // split: arrival counters per long row
+    uint32_t *scratch = nullptr;       // every other per-run array (one allocation)
     float *vals = nullptr;             // exact long rows: gathered terms (edge-indexed)
     uint32_t *rows = nullptr;          // rows with in-edges, then rows without
+    uint32_t *long_rows = nullptr;     // long rows by decreasing length
+    uint32_t *long_total = nullptr;    // device: number of long rows
+    uint32_t *giant_total = nullptr;   // device: how many of them exceed GIANT_ROW
+    uint32_t *sum_ctr = nullptr;       // k_pr_long_sums' job and finish counters
     const uint32_t *count_all = nullptr;       // device: items in the list
     const uint32_t *count_nonconst = nullptr;  // device: items before the CONST ones
 };
@@ -990,46 +1135,81 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
 
 int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &run, cudaStream_t s)
 {
-    const uint64_t n = g->vertex_count;
+    const uint64_t n = g->vertex_count, m = g->edge_count;
     if (n > ROW_MASK) return BW_ERR_TOO_LARGE;
     const uint64_t windows = (n + 31) / 32;
-    // Short items <= N + W; pieces <= M / SEG_EDGES + M / SEG_LONG; CONST <= W.
-    const uint64_t cap = 2 * windows + n + g->edge_count / SEG_EDGES + g->edge_count / SEG_LONG + 16;
-    // scan areas: row flags (N + 1) -> positions; window counts
-    // [pieces | short items | const items | 0] (3W + 1) -> first positions
-    const uint64_t entries = 3 * windows + 1;
-    size_t temp_rows = 0, temp_items = 0;
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp_rows, static_cast<uint32_t *>(nullptr),
+    const uint64_t lcap = m / (SEG_LONG + 1) + 1;          // long rows at most
+    // Pieces <= M / SEG_EDGES + lcap; short items <= N + W; CONST <= W.
+    const uint64_t cap = 2 * windows + n + m / SEG_EDGES + lcap + 16;
+    size_t t_scan_n = 0, t_scan_l = 0, t_scan_w = 0, t_sort = 0;
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_n, static_cast<uint32_t *>(nullptr),
                                           static_cast<uint32_t *>(nullptr), static_cast<int64_t>(n + 1), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, temp_items, static_cast<uint32_t *>(nullptr),
-                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(entries), s));
-    auto align64 = [](uint64_t words) { return (words + 63) & ~uint64_t(63); };   // 256-byte boundaries
-    const uint64_t at_pos = align64(n + 1), at_counts = at_pos + align64(n + 1),
-                   at_first = at_counts + align64(entries), at_temp = at_first + align64(entries);
-    const size_t temp = std::max(temp_rows, temp_items);
-    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.win_counts), at_temp * sizeof(uint32_t) + temp, s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_l, static_cast<uint32_t *>(nullptr),
+                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(lcap + 1), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_w, static_cast<uint32_t *>(nullptr),
+                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(2 * windows + 1), s));
+    cub::DoubleBuffer<uint32_t> lkeys(nullptr, nullptr), lids(nullptr, nullptr);
+    BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
+    const size_t temp = std::max(std::max(t_scan_n, t_scan_l), std::max(t_scan_w, t_sort));
+    // one allocation, 256-byte aligned regions (sizes in words)
+    auto al = [](uint64_t w) { return (w + 63) & ~uint64_t(63); };
+    uint64_t at = 0;
+    const uint64_t o_flag = at; at += al(n + 1);
+    const uint64_t o_pos = at; at += al(n + 1);
+    const uint64_t o_lflag = at; at += al(n + 1);
+    const uint64_t o_lpos = at; at += al(n + 1);
+    const uint64_t o_lkey0 = at; at += al(lcap);
+    const uint64_t o_lkey1 = at; at += al(lcap);
+    const uint64_t o_lid0 = at; at += al(lcap);
+    const uint64_t o_lid1 = at; at += al(lcap);
+    const uint64_t o_pcnt = at; at += al(lcap + 1);
+    const uint64_t o_ppos = at; at += al(lcap + 1);
+    const uint64_t o_wcnt = at; at += al(2 * windows + 1);
+    const uint64_t o_first = at; at += al(2 * windows + 1);
+    const uint64_t o_tot = at; at += al(5);
+    const uint64_t o_temp = at;
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.scratch), o_temp * sizeof(uint32_t) + temp, s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.rows), n * sizeof(uint32_t), s));
-    uint32_t *flags = run.win_counts, *pos = run.win_counts + at_pos;
-    uint32_t *counts = run.win_counts + at_counts, *first = run.win_counts + at_first;
-    void *scratch = run.win_counts + at_temp;
-    k_row_flags<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, flags);
-    BW_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(scratch, temp_rows, flags, pos, static_cast<int64_t>(n + 1), s));
-    k_row_partition<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, n, pos, run.rows);
-    k_seg_count<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, counts);
-    BW_CUDA(cudaMemsetAsync(counts + 3 * windows, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(scratch, temp_items, counts, first, static_cast<int64_t>(entries), s));
-    k_seg_emit<<<ctx->sm_count * 4, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, split, first, run.work,
-                                                  run.long_count);
-    ctx->launches += 4;                  // flags, partition, count, emit (the scans are the library's)
+    uint32_t *S = run.scratch;
+    void *tmp = S + o_temp;
+    uint32_t *flag = S + o_flag, *pos = S + o_pos, *lflag = S + o_lflag, *lpos = S + o_lpos;
+    uint32_t *pcnt = S + o_pcnt, *ppos = S + o_ppos, *wcnt = S + o_wcnt, *first = S + o_first, *tot = S + o_tot;
+    run.long_total = lpos + n;
+    run.giant_total = tot + 2;
+    run.sum_ctr = tot + 3;
+    const unsigned grid = ctx->sm_count * 4;
+    // 1. row classes and the partition
+    k_row_flags<<<grid, 256, 0, s>>>(g->rev_vertices, n, flag, lflag);
+    BW_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
+    BW_CUDA(cudaMemsetAsync(lflag + n, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, flag, pos, static_cast<int64_t>(n + 1), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, lflag, lpos, static_cast<int64_t>(n + 1), s));
+    BW_CUDA(cudaMemsetAsync(S + o_lkey0, 0, lcap * sizeof(uint32_t), s));   // past the last long row: length 0
+    k_row_partition<<<grid, 256, 0, s>>>(g->rev_vertices, n, pos, lpos, run.rows, S + o_lkey0, S + o_lid0);
+    // 2. long rows by decreasing length (stable), their pieces in that order
+    lkeys = cub::DoubleBuffer<uint32_t>(S + o_lkey0, S + o_lkey1);
+    lids = cub::DoubleBuffer<uint32_t>(S + o_lid0, S + o_lid1);
+    BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
+    run.long_rows = lids.Current();
+    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, pcnt);
+    BW_CUDA(cudaMemsetAsync(pcnt + lcap, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
+    k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
+                                      split, run.work, run.long_count, run.giant_total);
+    BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
+    // 3. short and CONST items after the pieces
+    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, wcnt);
+    BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
+    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_w, wcnt, first, static_cast<int64_t>(2 * windows + 1), s));
+    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, first, ppos + lcap, run.work, tot);
+    ctx->launches += 6;                  // flags, partition, piece count/emit, count, emit (scans, sort: library)
     BW_CUDA(cudaGetLastError());
-    // the list's length stays on the device (no host round trip in a run)
-    run.count_all = first + 3 * windows;
-    run.count_nonconst = first + 2 * windows;
-    if (!split && g->edge_count)
-        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), g->edge_count * sizeof(float), s));
+    run.count_nonconst = tot;
+    run.count_all = tot + 1;
+    if (!split && m)
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
     return BW_OK;
 }
 
@@ -1037,10 +1217,10 @@ void free_run(PrRun &run, cudaStream_t s)
 {
     if (run.work) cudaFreeAsync(run.work, s);
     if (run.long_count) cudaFreeAsync(run.long_count, s);
-    if (run.win_counts) cudaFreeAsync(run.win_counts, s);
+    if (run.scratch) cudaFreeAsync(run.scratch, s);
     if (run.vals) cudaFreeAsync(run.vals, s);
     if (run.rows) cudaFreeAsync(run.rows, s);
-    run.work = nullptr; run.long_count = nullptr; run.win_counts = nullptr; run.vals = nullptr; run.rows = nullptr;
+    run = PrRun{};
 }
 
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
@@ -1055,10 +1235,14 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_VERTEX_PULL:
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        k_pr_long_sums<false><<<ctx->sm_count * 4, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        ctx->launches++;
         break;
       case PR_VERTEX_PULL_NODIV:
         if (geo.block == PULL_WIDE) k_pr_pull_items<true, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<true, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        k_pr_long_sums<true><<<ctx->sm_count * 4, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        ctx->launches++;
         break;
       case PR_VERTEX_PULL_WARP: k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
       case PR_VERTEX_PULL_WARP_NODIV: k_pr_vertex_pull_warp<true><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
@@ -1277,6 +1461,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.long_count = items.long_count;
         a.vals = items.vals;
         a.rows = items.rows;
+        a.long_rows = items.long_rows;
+        a.long_total = items.long_total;
+        a.giant_total = items.giant_total;
+        a.sum_ctr = items.sum_ctr;
         // div: rows without in-edges hold the same rank and contribution in
         // both buffers once iterations 1 and 2 have written them
         a.count_dev = items.work ? ((!nodiv && j > 2) ? items.count_nonconst : items.count_all) : nullptr;

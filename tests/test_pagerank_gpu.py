@@ -65,11 +65,28 @@ def test_variant_parity(ctx, graphs, variant, iterations):
         assert _rel(got, r64) <= REL_F64, (name, gname)
 
 
+def _chosen_in_degrees(n=80000, seed=9):
+    """In-rows of chosen lengths around every boundary of the long-row paths
+    (pieces of 512, batches of rows up to 4096 terms, whole-warp rows above
+    it), sources drawn at random with varied out-degrees."""
+    rng = np.random.default_rng(seed)
+    lengths = [1, 255, 256, 257, 300, 511, 512, 513, 1023, 1024, 1025, 4095, 4096, 4097, 5000, 20000]
+    lengths += list(rng.integers(257, 4096, 70))
+    src, dst = [], []
+    for v, d in enumerate(lengths):
+        src.append(rng.choice(np.arange(len(lengths), n), size=d, replace=False))
+        dst.append(np.full(d, v))
+    src.append(rng.integers(len(lengths), n, 200000))      # background edges
+    dst.append(rng.integers(len(lengths), n, 200000))      # the chosen rows keep their lengths
+    return bw.HostGraph.from_edges(n, np.concatenate(src).astype(np.uint32), np.concatenate(dst).astype(np.uint32))
+
+
 @pytest.fixture(scope="module")
 def long_graphs(ctx):
     from tests.graphs import star_in
     out = {}
-    for kind, h in (("star_in", star_in(200000)), ("rmat16", bw.HostGraph.rmat(16, 32, seed=3))):
+    for kind, h in (("star_in", star_in(200000)), ("rmat16", bw.HostGraph.rmat(16, 32, seed=3)),
+                    ("chosen", _chosen_in_degrees())):
         out[kind] = (h, bw.DeviceGraph(h))
     return out
 
@@ -77,23 +94,23 @@ def long_graphs(ctx):
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
 @pytest.mark.parametrize("iterations", [1, 2, 30])
 def test_long_rows(ctx, long_graphs, variant, iterations):
-    """In-rows far longer than one work item: the exact variants evaluate
-    the sequential sum with the whole warp and must stay bit-identical,
-    including a 199,999-term row of equal terms (a round-half-even tie at
-    nearly every step) and R-MAT hubs.  On the equal-term row the
-    reference's own loop is far from FP64 (1.2e-3 after one iteration, 2e-5
-    after 30), so there the exact variants are held to the reference bits
-    only and pull-segmented, which reorders the sum, to FP64 only; on the
-    R-MAT graph every bound applies."""
+    """In-rows far longer than one work item, on every path the exact
+    variants take (batches of rows up to 4096 terms summed one row per lane,
+    longer rows summed by a whole warp), including a 199,999-term row of
+    equal terms (a round-half-even tie at nearly every step), rows at every
+    length boundary and R-MAT hubs: bit-identical to the reference.  The
+    reference's own loop can be far from FP64 on such rows (1.2e-3 after one
+    iteration on the equal-term row), so pull-segmented, which reorders the
+    sum, is held to the reference only where the reference is within 1e-5
+    of FP64, and to FP64 everywhere."""
     for kind, (h, g) in long_graphs.items():
         got = bw.pagerank(ctx, g, variant, iterations).ranks.cpu().numpy()
         div, nodiv, d64, n64 = _oracles(h, iterations)
         ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
         if variant in BITEXACT:
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, kind)
-            if kind == "star_in":
-                continue
-        elif kind != "star_in":
+            continue
+        if _rel(ref, r64) <= REL_REF:
             assert _rel(got, ref) <= REL_REF, (variant, kind)
         assert _rel(got, r64) <= REL_F64, (variant, kind)
 
@@ -108,11 +125,11 @@ def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs, relabel):
     any of them."""
     for name, (h, g) in list(long_graphs.items()) + [("rmat14", graphs["rmat14"]), ("chain", graphs["chain"])]:
         got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs, relabel=relabel).ranks.cpu().numpy()
-        div, nodiv, _, _ = _oracles(h, 30)
-        ref = nodiv if "nodiv" in variant else div
+        div, nodiv, d64, n64 = _oracles(h, 30)
+        ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
         if variant in BITEXACT:
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name, block, hubs)
-        elif name != "star_in":
+        elif _rel(ref, r64) <= REL_REF:
             assert _rel(got, ref) <= REL_REF, (variant, name, block, hubs)
 
 
@@ -148,17 +165,19 @@ def test_diffs_reported(ctx, graphs):
 
 def test_kernel_launch_count(ctx, graphs, long_graphs):
     """The run reports exactly the kernels of this library it launched:
-    degrees (row lengths), work list (row flags, partition, count, emit),
-    the hub-first order (keys, the device-side decision unless forced,
-    slots, source translation -- the last two return at once when the
-    order is not taken), init, one kernel per fused iteration or two
-    (scatter + consolidation) otherwise."""
+    degrees (row lengths), work list (row classes, partition, long-row
+    piece count and emission, short-item count and emission), the
+    hub-first order (keys, the device-side decision unless forced, slots,
+    source translation -- the last two return at once when the order is not
+    taken), init, and per iteration one kernel for pull-segmented, two for
+    the exact variants (work list + long-row sums) and for the atomic ones
+    (scatter + consolidation)."""
     _, g = graphs["rmat14"]
-    assert bw.pagerank(ctx, g, "vertex-pull", 5).kernel_launches == 1 + 4 + 4 + 1 + 5
-    assert bw.pagerank(ctx, g, "vertex-pull", 2).kernel_launches == 1 + 4 + 1 + 2
+    assert bw.pagerank(ctx, g, "vertex-pull", 5).kernel_launches == 1 + 6 + 4 + 1 + 2 * 5
+    assert bw.pagerank(ctx, g, "vertex-pull", 2).kernel_launches == 1 + 6 + 1 + 2 * 2
     assert bw.pagerank(ctx, g, "rev-edge-list", 5).kernel_launches == 1 + 1 + 2 * 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 4 + 3 + 1 + 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 4 + 1 + 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 6 + 3 + 1 + 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 6 + 1 + 5
 
 
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented", "vertex-pull-warp"])
@@ -175,9 +194,9 @@ def test_reverse_only_view(ctx, graphs, long_graphs, variant):
             vertex_count, edge_count = g.vertex_count, g.edge_count
             view = _abi.GraphView(v.vertex_count, v.edge_count, 0, 0, v.rev_vertices, v.rev_edges, 0, 0, 0, 0)
         got = bw.pagerank(ctx, RevOnly, variant, 30).ranks.cpu().numpy()
-        div, nodiv, _, _ = _oracles(h, 30)
-        ref = nodiv if "nodiv" in variant else div
+        div, nodiv, d64, n64 = _oracles(h, 30)
+        ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
         if variant in BITEXACT:
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name)
-        elif name != "star_in":
+        elif _rel(ref, r64) <= REL_REF:
             assert _rel(got, ref) <= REL_REF, (variant, name)

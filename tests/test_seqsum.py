@@ -1,9 +1,10 @@
 """The warp-parallel evaluation of a sequential float sum (csrc/bw_seqsum.h)
 against the plain loop s = fl(s + x[i]) on the CPU.
 
-The checker emulates the warp algorithm the PageRank kernel runs on long
-rows (32 lanes x 8 terms per window, map scan, binade crossings found by one
-lane) with the header's helpers, and compares the bits of the result with a
+The checker emulates the warp algorithm the PageRank kernels run on the
+longest rows (32 lanes x 8 or 32 terms per window, per-lane map
+composition, lane scan, binade crossings found by one lane) with the
+header's helpers, and compares the bits of the result with a
 sequential float loop compiled with -ffp-contract=off.  Inputs cover wide
 dynamic ranges, long runs of equal terms (which hit round-half-even ties
 at every step once the sum is large), constructed ties, zeros, leading
@@ -33,13 +34,16 @@ static uint32_t sequential(const std::vector<float> &x) {
 }
 
 // Terms added in order by one lane before the map scan takes over (the
-// kernel's SERIAL_TERMS); the checker runs several values, including ones
-// that end inside a window.
+// kernel's SERIAL_TERMS), and terms per lane (the window is 32 x L; with
+// L > 8 a lane composes its maps as a tree of branch-free steps, as the
+// wide kernel does); the checker runs several settings, including serial
+// starts that end inside a window.
 static uint32_t serial_terms = 0;
+static uint32_t L = 8;
 
 // Warp emulation; returns false when the kernel would fall back.
 static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
-    const uint32_t L = 8, WIN = 32 * L, n = vals.size();
+    const uint32_t WIN = 32 * L, n = vals.size();
     uint32_t sb = 0;
     for (uint32_t w = 0; w < n; w += WIN) {
         uint32_t pos = 0;
@@ -50,7 +54,7 @@ static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
             sb = fb(acc);
             pos = i - w;
         }
-        uint32_t x[32][8];
+        uint32_t x[32][32];
         for (uint32_t lane = 0; lane < 32; lane++)
             for (uint32_t u = 0; u < L; u++) {
                 const uint32_t k = lane * L + u;
@@ -77,6 +81,19 @@ static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
             const uint32_t K = exponent_of(sb), A = significand_of(sb);
             Map m[32];
             for (uint32_t lane = 0; lane < 32; lane++) {
+                if (L > 8) {                       // branch-free steps composed as a tree
+                    Map t[32];
+                    bool good = true;
+                    for (uint32_t u = 0; u < L; u++) {
+                        const uint32_t i = lane * L + u;
+                        t[u] = step_select(i >= pos && i < lim ? x[lane][u] : 0u, K, good);
+                    }
+                    if (!good) return false;
+                    for (uint32_t st = 1; st < L; st <<= 1)
+                        for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
+                    m[lane] = t[0];
+                    continue;
+                }
                 m[lane] = identity();
                 for (uint32_t u = 0; u < L; u++) {
                     const uint32_t i = lane * L + u;
@@ -150,7 +167,8 @@ static void check(const std::vector<float> &x, bool expect_domain) {
 static void run_all();
 
 int main() {
-    for (uint32_t st : {0u, 64u, 300u, 1024u}) { serial_terms = st; run_all(); }
+    for (uint32_t l : {8u, 32u})
+        for (uint32_t st : {0u, 64u, 300u, 1024u}) { L = l; serial_terms = st; run_all(); }
     std::printf("tested %d fallback %d bad %d\n", tested, fallback, bad);
     return bad ? 1 : 0;
 }
@@ -238,3 +256,43 @@ def test_warp_sequential_sum_matches_loop(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stdout[-3000:]
     assert "bad 0" in out.stdout
+
+
+STEP_CHECK = r"""
+#include <cstdio>
+#include <cstdint>
+#include "bw_seqsum.h"
+using namespace bwseq;
+static uint64_t rng = 0x9e3779b97f4a7c15ULL;
+static uint64_t nxt() { rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17; return rng; }
+int main() {
+    long bad = 0, n = 0;
+    for (long i = 0; i < 20000000; i++) {
+        uint32_t xb = static_cast<uint32_t>(nxt());
+        if (i % 7 == 0) xb &= 0x807fffffu;            // zero exponent: zeros and subnormals
+        if (i % 11 == 0) xb = 0;
+        const uint32_t k = 1 + static_cast<uint32_t>(nxt() % 254);
+        Map a; const bool oka = step(xb, k, a);
+        bool okb = true; const Map b = step_select(xb, k, okb);
+        n++;
+        if (oka != okb || (oka && (a.e != b.e || a.o != b.o))) {
+            if (bad < 5) std::printf("x=%08x k=%u step=(%u,%u,%d) select=(%u,%u,%d)\n", xb, k, a.e, a.o, oka, b.e, b.o, okb);
+            bad++;
+        }
+    }
+    std::printf("tested %ld bad %ld\n", n, bad);
+    return bad ? 1 : 0;
+}
+"""
+
+
+def test_branch_free_step_matches(tmp_path):
+    """step_select (the wide kernel's branch-free form) equals step on 20M
+    random terms and binades, including zeros, subnormals, negatives and
+    inf/NaN."""
+    src = tmp_path / "step.cpp"
+    src.write_text(STEP_CHECK)
+    exe = tmp_path / "step"
+    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{HEADER.parent}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stdout[-2000:]
