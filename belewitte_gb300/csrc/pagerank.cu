@@ -86,7 +86,10 @@ struct PrArgs {
     const uint32_t *rows;      // work-list kernels: rows with in-edges, then rows without
     const uint32_t *long_rows;    // exact variants: long rows by decreasing length
     const uint32_t *long_total;   // device: number of long rows
-    const uint32_t *giant_total;  // device: long rows summed by a whole warp (the first ones)
+    const uint32_t *giant_total;  // device: long rows summed piece-parallel (the first ones)
+    const uint32_t *giant_pieces; // device: their pieces (work items [0, giant_pieces))
+    float *piece_sum;             // exact pieces: float sum of the piece's terms (any order)
+    uint4 *piece_map;             // giant-row pieces: two-uint4 records (k_pr_long_sums)
     uint32_t *sum_ctr;            // k_pr_long_sums' job and finish counters
     // Decided on the device, so the host never waits inside a run:
     const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
@@ -546,17 +549,20 @@ __global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint3
         pieces[i] = i < L ? (long_len[i] + SEG_EDGES - 1) / SEG_EDGES : 0u;
 }
 
-// Exact long rows above GIANT_ROW terms are summed by a whole warp (binade
-// maps over coalesced windows); shorter ones in batches of 32, one row per
-// lane.
-constexpr uint32_t GIANT_ROW = 4096;
+// Exact long rows above GIANT_ROW terms are summed piece-parallel (binade
+// maps per piece, combined by the row's last piece); shorter ones in
+// batches of 32, one row per lane.  A lane's row is a chain of dependent
+// additions whose loads it can hold only a few dozen terms ahead: measured
+// on GB300 at about 29 cycles a term, which bounds the shorter rows' length.
+constexpr uint32_t GIANT_ROW = 2048;
 
-// Pieces of sorted long row i at [ppos[i], ppos[i + 1]); the split
-// variant's arrival counters cleared; the number of rows above GIANT_ROW.
+// Pieces of sorted long row i at [ppos[i], ppos[i + 1]); the arrival
+// counters cleared; the number of rows above GIANT_ROW and of their pieces.
 __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ long_row,
                              const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
                              const uint32_t *__restrict__ ppos, int split, uint4 *__restrict__ work,
-                             uint32_t *__restrict__ long_count, uint32_t *__restrict__ giant_total)
+                             uint32_t *__restrict__ long_count, uint32_t *__restrict__ giant_total,
+                             uint32_t *__restrict__ giant_pieces)
 {
     const uint64_t L = *long_total;
     uint64_t lo = 0, hi = L;                       // giant rows come first (lengths decrease)
@@ -564,7 +570,10 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
         const uint64_t mid = (lo + hi) / 2;
         if (long_len[mid] > GIANT_ROW) lo = mid + 1; else hi = mid;
     }
-    if (gtid() == 0) *giant_total = static_cast<uint32_t>(lo);
+    if (gtid() == 0) {
+        *giant_total = static_cast<uint32_t>(lo);
+        *giant_pieces = ppos[lo];
+    }
     const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
     for (uint64_t i = gtid(); i < L; i += gthreads()) {
         const uint32_t r = long_row[i];
@@ -720,32 +729,34 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
     }
 }
 
-// The sequential sum s = fl(s + vals[i]), i = 0..n-1, starting from +0 --
-// bit-identical to one thread's loop -- evaluated window by window
-// (32 x L terms, staged in shared memory, the next window's loads in
-// flight).  The first SERIAL_TERMS terms are added by lane 0 in order:
-// there the sum doubles every few terms, and a binade crossing costs the
-// map scan a restart.  The rest uses the binade maps of bw_seqsum.h: each
-// lane composes the maps of its L consecutive terms as a tree (depth
-// log2 L, branch-free steps), the warp scans the lanes' maps, and the lane
-// that holds the next binade crossing adds that term with one float
-// addition.  `stage` holds 33 x L floats of shared memory per warp; `vals`
-// was written by the previous kernel, so it is read through L2.  Every lane
-// returns the sum.
+// The sequential sum s = fl(s + vals[i]) over i = b..e-1, continued from
+// the running sum with bits `sb` -- bit-identical to one thread's loop --
+// evaluated window by window (32 x L terms, staged in shared memory, the
+// next window's loads in flight).  Terms at row positions below
+// SERIAL_TERMS are added by lane 0 in order: there the sum doubles every
+// few terms, and a binade crossing costs the map scan a restart.  The rest
+// uses the binade maps of bw_seqsum.h: each lane composes the maps of its L
+// consecutive terms as a tree (depth log2 L, branch-free steps), the warp
+// scans the lanes' maps, and the lane that holds the next binade crossing
+// adds that term with one float addition.  `stage` holds 33 x L floats of
+// shared memory per warp; `vals` (the row's terms, position 0 first) was
+// written by the previous kernel, so it is read through L2.  False when a
+// term or the sum leaves the maps' domain (the caller then runs the plain
+// loop); `sb` is warp-uniform.
 constexpr uint32_t SERIAL_TERMS = 1024;   // measured: 64 was 23% slower on R-MAT-22
 
 template<uint32_t L>
-__device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t n, float *stage, unsigned lane)
+__device__ __forceinline__ bool warp_sequential_continue(const float *vals, uint32_t b, uint32_t e, uint32_t &sb,
+                                                         float *stage, unsigned lane)
 {
     using namespace bwseq;
     static_assert((L & (L - 1)) == 0 && L <= 32, "L: a power of two up to 32");
     constexpr uint32_t WIN = 32 * L;
-    uint32_t sb = 0;                       // bits of the running sum (warp-uniform)
     bool ok = true;
     float pre[L];
 #pragma unroll
-    for (uint32_t u = 0; u < L; u++) pre[u] = u * 32 + lane < n ? __ldcg(vals + u * 32 + lane) : 0.0f;
-    for (uint32_t w = 0; w < n && ok; w += WIN) {
+    for (uint32_t u = 0; u < L; u++) pre[u] = b + u * 32 + lane < e ? __ldcg(vals + b + u * 32 + lane) : 0.0f;
+    for (uint32_t w = b; w < e && ok; w += WIN) {
         // window [w, w + WIN): coalesced loads, staged so that lane l reads
         // terms l*L .. l*L + L-1 (element k at k + k / 32: no bank conflicts)
 #pragma unroll
@@ -760,8 +771,8 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
         const uint32_t nw = w + WIN;
 #pragma unroll
         for (uint32_t u = 0; u < L; u++)
-            pre[u] = nw + u * 32 + lane < n ? __ldcg(vals + nw + u * 32 + lane) : 0.0f;
-        const uint32_t lim = min(WIN, n - w), first = lane * L;
+            pre[u] = nw + u * 32 + lane < e ? __ldcg(vals + nw + u * 32 + lane) : 0.0f;
+        const uint32_t lim = min(WIN, e - w), first = lane * L;
         uint32_t pos = 0;                  // first term of the window not yet added
         if (w < SERIAL_TERMS) {            // early terms: lane 0 adds them in order
             const uint32_t upto = min(lim, SERIAL_TERMS - w);
@@ -833,12 +844,12 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
                     if (np == 0 && first + u >= pos && first + u < lim) {
                         Map tu;
                         step(x[u], K, tu);
-                        const uint32_t b = apply(tu, acc);
-                        if (b >= TOP) {
+                        const uint32_t bu = apply(tu, acc);
+                        if (bu >= TOP) {
                             nb = __float_as_uint(__fadd_rn(__uint_as_float(bits_of(K, acc)), __uint_as_float(x[u])));
                             np = first + u + 1;
                         } else {
-                            acc = b;
+                            acc = bu;
                         }
                     }
                 }
@@ -849,13 +860,17 @@ __device__ __forceinline__ float warp_sequential_sum(const float *vals, uint32_t
             pos = np;
         }
     }
-    if (!ok) {                             // outside the domain: the plain loop
-        float s = 0.0f;
-        if (lane == 0)
-            for (uint32_t i = 0; i < n; i++) s = __fadd_rn(s, __ldcg(vals + i));
-        return __shfl_sync(FULL_MASK, s, 0);
-    }
-    return __uint_as_float(sb);
+    return ok;
+}
+
+// One lane's plain loop over the row (terms outside the maps' domain);
+// every lane returns the sum.
+__device__ __forceinline__ float warp_plain_sum(const float *vals, uint32_t n, unsigned lane)
+{
+    float s = 0.0f;
+    if (lane == 0)
+        for (uint32_t i = 0; i < n; i++) s = __fadd_rn(s, __ldcg(vals + i));
+    return __shfl_sync(FULL_MASK, s, 0);
 }
 
 template<bool NODIV, bool EXACT_LONG, int BLOCK>
@@ -913,9 +928,12 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
             continue;
         }
         if (EXACT_LONG && (w.y & LONG_FLAG)) {
-            // exact piece: store the gathered terms in edge order; the
-            // long-row sums run in k_pr_long_sums after this kernel
+            // exact piece: store the gathered terms in edge order (the
+            // long-row sums run in k_pr_long_sums after this kernel) and
+            // their float sum in any order, from which the pieces of giant
+            // rows guess the running sum of the row
             const uint32_t len = e1 - e0;
+            float part = 0.0f;
             for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
                 uint32_t idx[GATHER_UNROLL];
 #pragma unroll
@@ -926,9 +944,15 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
 #pragma unroll
                 for (int u = 0; u < GATHER_UNROLL; u++) {
                     const uint32_t k = base + u * 32 + lane;
-                    if (k < len) __stcg(a.vals + e0 + k, gather1(src, hub, hubs, idx[u]));
+                    if (k < len) {
+                        const float v = gather1(src, hub, hubs, idx[u]);
+                        __stcg(a.vals + e0 + k, v);
+                        part += v;
+                    }
                 }
             }
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
+            if (lane == 0) a.piece_sum[it] = part;   // pieces lead the list: item = piece
             continue;
         }
         // up to 32 rows rows[r0 + l]: lane l owns one; its row end and
@@ -960,24 +984,288 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_p
 
 // Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
 // after the iteration's work-list kernel has stored every long row's terms
-// in vals[] (edge order).  Jobs are taken in order from a counter (no static
-// share, so a warp that drew a long job takes fewer): first the rows above
-// GIANT_ROW terms, longest first, each summed by one warp
-// (warp_sequential_sum); then batches of 32 shorter long rows of similar
-// length, one row per lane (lane_sequential_sum).  Every sum is the
-// reference's sequential loop, bit-identical.  The last warp to finish
-// resets the counters for the next iteration.
+// in vals[] (edge order) and every piece's float sum in piece_sum[].  Jobs
+// are taken in order from a counter (no static share, so a warp that drew a
+// long job takes fewer):
+//  * first batches of 32 long rows of at most GIANT_ROW terms and similar
+//    length, one row per lane (lane_sequential_sum): the longest chains of
+//    dependent additions start first.
+//  * then the pieces of the rows above GIANT_ROW terms, longest rows
+//    first.  Piece 0 adds the row's first SERIAL_TERMS terms in order (one
+//    lane, from shared memory).  Every later piece guesses the running sum at its start (the
+//    float sums of the pieces before it, added in double) and records, in
+//    the guessed binade, the map of its terms -- or, when the guess crosses
+//    into the next binade inside the piece, the map of the terms before the
+//    crossing term, that term, and the map of the terms after it in the new
+//    binade.  The row's last piece to finish combines the records in order,
+//    scanning runs of map records with the warp: a record that holds for
+//    the true running sum (same binade, crossing where recorded) is applied,
+//    any other piece is evaluated exactly from the true running sum
+//    (warp_sequential_continue).  The guesses only decide how much work the
+//    combination does, never its result.
+// Every sum is the reference's sequential loop, bit-identical.  The last
+// warp to finish resets the job counters for the next iteration; each
+// giant row's combining piece resets the row's arrival counter.
 constexpr int LONG_SUM_THREADS = 256;
-constexpr uint32_t TERMS_PER_LANE = 32;      // warp-sum windows of 1024 terms
+constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
+constexpr uint32_t PIECE_L = SEG_EDGES / 32;        // terms per lane: one window per piece
+constexpr uint32_t SERIAL_PIECES = SERIAL_TERMS / SEG_EDGES;
+static_assert(SERIAL_TERMS % SEG_EDGES == 0, "the serial start covers whole pieces");
+static_assert(GIANT_ROW >= SERIAL_TERMS, "giant rows go past the serial start");
+// Piece records, two uint4 per piece: r0 = {kind | tg << 8, K | K2 << 8, M1.e, M1.o},
+// r1 = {bits of term tg, M2.e, M2.o, 0}
+constexpr uint32_t REC_NONE = 0;      // evaluated exactly by the combination
+constexpr uint32_t REC_BINADE = 1;    // M1: the piece's terms in binade K
+constexpr uint32_t REC_STATE = 2;     // r0.y: the running sum after the serial start
+constexpr uint32_t REC_CROSS = 3;     // M1: terms before tg in K; tg crosses into K2; M2: the rest in K2
+
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t *p, uint32_t v)
+{
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// The sum of rv[0, SERIAL_TERMS) in row order: coalesced loads of the whole
+// range, then lane 0 adds the terms from shared memory (four per load).
+// `stage` is 16-byte aligned and holds 32 x PIECE_L floats.
+__device__ __forceinline__ uint32_t warp_serial_start(const float *rv, float *stage, unsigned lane)
+{
+    constexpr uint32_t HALF = 32 * PIECE_L;
+    static_assert(SERIAL_TERMS == 2 * HALF, "the serial start is two stages");
+    float v[2][PIECE_L];
+#pragma unroll
+    for (uint32_t h = 0; h < 2; h++)
+#pragma unroll
+        for (uint32_t u = 0; u < PIECE_L; u++) v[h][u] = __ldcg(rv + h * HALF + u * 32 + lane);
+    float acc = 0.0f;
+#pragma unroll
+    for (uint32_t h = 0; h < 2; h++) {
+#pragma unroll
+        for (uint32_t u = 0; u < PIECE_L; u++) stage[u * 32 + lane] = v[h][u];
+        __syncwarp();
+        if (lane == 0) {
+            const float4 *s4 = reinterpret_cast<const float4 *>(stage);
+#pragma unroll 8
+            for (uint32_t i = 0; i < HALF / 4; i++) {
+                const float4 q = s4[i];
+                acc = __fadd_rn(acc, q.x); acc = __fadd_rn(acc, q.y);
+                acc = __fadd_rn(acc, q.z); acc = __fadd_rn(acc, q.w);
+            }
+        }
+        __syncwarp();
+    }
+    return __shfl_sync(FULL_MASK, __float_as_uint(acc), 0);
+}
+
+// Ordered composition of the lanes' maps; lane 0 ends with all of them.
+__device__ __forceinline__ bwseq::Map warp_compose(bwseq::Map m, unsigned lane)
+{
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const bwseq::Map y{__shfl_down_sync(FULL_MASK, m.e, o), __shfl_down_sync(FULL_MASK, m.o, o)};
+        if ((lane & (2 * o - 1)) == 0) m = bwseq::compose(m, y);
+    }
+    return m;
+}
+
+// A lane's PIECE_L maps of terms x in binade K composed as a tree (with
+// skip != ~0, the terms at positions first + u <= skip are replaced by +0,
+// the identity).
+__device__ __forceinline__ bwseq::Map lane_maps(const uint32_t (&x)[PIECE_L], uint32_t K, uint32_t first,
+                                                uint32_t skip, bool &good)
+{
+    using namespace bwseq;
+    Map t[PIECE_L];
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++)
+        t[u] = step_select(skip == 0xffffffffu || first + u > skip ? x[u] : 0u, K, good);
+#pragma unroll
+    for (uint32_t st = 1; st < PIECE_L; st <<= 1) {
+#pragma unroll
+        for (uint32_t u = 0; u + st < PIECE_L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
+    }
+    return t[0];
+}
+
+// The record of piece q >= SERIAL_PIECES of a giant row (valid in lane 0).
+__device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0, uint32_t q,
+                                             float *stage, unsigned lane, uint4 &r0, uint4 &r1)
+{
+    using namespace bwseq;
+    r0 = make_uint4(REC_NONE, 0u, 0u, 0u);
+    r1 = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t b = q * SEG_EDGES, len = min(SEG_EDGES, n - b);
+    float v[PIECE_L];                                // the terms, coalesced (issued first)
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) {
+        const uint32_t k = u * 32 + lane;
+        v[u] = k < len ? __ldcg(rv + b + k) : 0.0f;
+    }
+    constexpr uint32_t PRE_U = 4;                    // the guess: earlier pieces' sums in double
+    double pre = 0.0;
+    for (uint32_t i0 = 0; i0 < q; i0 += 32 * PRE_U) {
+        float f[PRE_U];
+#pragma unroll
+        for (uint32_t k = 0; k < PRE_U; k++) {
+            const uint32_t i = i0 + k * 32 + lane;
+            f[k] = i < q ? __ldcg(a.piece_sum + p0 + i) : 0.0f;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < PRE_U; k++) pre += static_cast<double>(f[k]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
+    // restage so that lane l holds terms l*PIECE_L .. (element k at k + k / 32)
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) stage[u * 33 + lane] = v[u];
+    __syncwarp();
+    uint32_t x[PIECE_L];
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) {
+        const uint32_t k = lane * PIECE_L + u;
+        x[u] = __float_as_uint(stage[k + (k >> 5)]);   // past the end: +0, the identity
+    }
+    __syncwarp();
+    const uint32_t guess = __float_as_uint(__double2float_rn(pre));
+    if (!in_domain(guess)) return;
+    const uint32_t K = exponent_of(guess), first = lane * PIECE_L;
+    bool good = true;
+    const Map m = lane_maps(x, K, first, 0xffffffffu, good);
+    if (__any_sync(FULL_MASK, !good)) return;
+    Map incl = m;                                     // lanes' maps scanned
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Map y{__shfl_up_sync(FULL_MASK, incl.e, o), __shfl_up_sync(FULL_MASK, incl.o, o)};
+        if (lane >= static_cast<unsigned>(o)) incl = compose(y, incl);
+    }
+    Map excl{__shfl_up_sync(FULL_MASK, incl.e, 1), __shfl_up_sync(FULL_MASK, incl.o, 1)};
+    if (lane == 0) excl = identity();
+    const uint32_t a0 = apply(excl, significand_of(guess)), a1 = apply(m, a0);
+    const unsigned cross = __ballot_sync(FULL_MASK, a1 >= TOP);
+    if (!cross) {
+        r0 = make_uint4(REC_BINADE, K, __shfl_sync(FULL_MASK, incl.e, 31), __shfl_sync(FULL_MASK, incl.o, 31));
+        return;
+    }
+    // the guessed crossing: the first lane whose run leaves the binade finds the term
+    const unsigned f = __ffs(cross) - 1;
+    uint32_t tg = 0, xb = 0, nb = 0;
+    Map pm = identity();
+    if (lane == f) {
+        uint32_t acc = a0;
+        bool found = false;
+#pragma unroll
+        for (uint32_t u = 0; u < PIECE_L; u++) {
+            if (!found) {
+                Map st;
+                step(x[u], K, st);
+                const uint32_t bu = apply(st, acc);
+                if (bu >= TOP) {
+                    found = true;
+                    tg = first + u;
+                    xb = x[u];
+                    nb = __float_as_uint(__fadd_rn(__uint_as_float(bits_of(K, acc)), __uint_as_float(x[u])));
+                } else {
+                    acc = bu;
+                    pm = compose(pm, st);
+                }
+            }
+        }
+    }
+    tg = __shfl_sync(FULL_MASK, tg, f);
+    xb = __shfl_sync(FULL_MASK, xb, f);
+    nb = __shfl_sync(FULL_MASK, nb, f);
+    const Map m1 = compose(Map{__shfl_sync(FULL_MASK, excl.e, f), __shfl_sync(FULL_MASK, excl.o, f)},
+                           Map{__shfl_sync(FULL_MASK, pm.e, f), __shfl_sync(FULL_MASK, pm.o, f)});
+    if (!in_domain(nb)) return;
+    const uint32_t K2 = exponent_of(nb);
+    const Map m2 = warp_compose(lane_maps(x, K2, first, tg, good), lane);   // the terms after tg
+    r0 = make_uint4(REC_CROSS | (tg << 8), K | (K2 << 8), m1.e, m1.o);
+    r1 = make_uint4(xb, m2.e, m2.o, 0u);
+}
+
+// Piece q from the running sum `sb`: its record when it holds for that sum,
+// else the exact evaluation of its terms.  False when a term or the sum
+// leaves the maps' domain.
+__device__ __forceinline__ bool piece_advance(const float *rv, uint32_t n, uint32_t q, const uint4 &r0,
+                                              const uint4 &r1, uint32_t &sb, float *stage, unsigned lane)
+{
+    using namespace bwseq;
+    const uint32_t kind = r0.x & 0xffu, K = r0.y & 0xffu;
+    if ((kind == REC_BINADE || kind == REC_CROSS) && in_domain(sb) && exponent_of(sb) == K) {
+        const uint32_t a1 = apply(Map{r0.z, r0.w}, significand_of(sb));
+        if (kind == REC_BINADE && a1 < TOP) {
+            sb = bits_of(K, a1);
+            return true;
+        }
+        Map st;
+        if (kind == REC_CROSS && a1 < TOP && step(r1.x, K, st) && apply(st, a1) >= TOP) {
+            const uint32_t nb = __float_as_uint(__fadd_rn(__uint_as_float(bits_of(K, a1)), __uint_as_float(r1.x)));
+            const uint32_t K2 = (r0.y >> 8) & 0xffu;
+            if (in_domain(nb) && exponent_of(nb) == K2) {
+                const uint32_t a3 = apply(Map{r1.y, r1.z}, significand_of(nb));
+                if (a3 < TOP) {
+                    sb = bits_of(K2, a3);
+                    return true;
+                }
+            }
+        }
+    }
+    const uint32_t b = q * SEG_EDGES;
+    return warp_sequential_continue<PIECE_L>(rv, b, min(n, b + SEG_EDGES), sb, stage, lane);
+}
+
+// The row's sum from the records of its pieces p0 .. p0 + pieces - 1 (the
+// warp of the last piece to finish).  Groups of 32 records: the run of map
+// records in the current sum's binade is applied with one scan, up to the
+// first piece it cannot take, which piece_advance takes.
+__device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0,
+                                                uint32_t pieces, float *stage, unsigned lane)
+{
+    using namespace bwseq;
+    const uint4 *rec = a.piece_map + 2 * static_cast<uint64_t>(p0);
+    uint32_t sb = __ldcg(rec).y;                     // REC_STATE of piece 0
+    bool ok = true;
+    for (uint32_t g = SERIAL_PIECES; g < pieces && ok; g += 32) {
+        const uint32_t cnt = min(32u, pieces - g);
+        const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+        const uint4 r0 = lane < cnt ? __ldcg(rec + 2 * (g + lane)) : zero;
+        const uint4 r1 = lane < cnt ? __ldcg(rec + 2 * (g + lane) + 1) : zero;
+        uint32_t pos = 0;
+        while (pos < cnt && ok) {
+            const uint32_t K = exponent_of(sb);
+            const bool live = lane >= pos && lane < cnt;
+            const bool simple = live && in_domain(sb) && (r0.x & 0xffu) == REC_BINADE && (r0.y & 0xffu) == K;
+            Map incl = simple ? Map{r0.z, r0.w} : identity();
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const Map y{__shfl_up_sync(FULL_MASK, incl.e, o), __shfl_up_sync(FULL_MASK, incl.o, o)};
+                if (lane >= static_cast<unsigned>(o)) incl = compose(y, incl);
+            }
+            const uint32_t av = apply(incl, significand_of(sb));
+            const unsigned stops = __ballot_sync(FULL_MASK, live && (!simple || av >= TOP));
+            const uint32_t s = stops ? __ffs(stops) - 1 : cnt;
+            if (s > pos) sb = bits_of(K, __shfl_sync(FULL_MASK, av, s - 1));   // pieces pos .. s-1
+            if (s >= cnt) break;
+            const uint4 q0{__shfl_sync(FULL_MASK, r0.x, s), __shfl_sync(FULL_MASK, r0.y, s),
+                           __shfl_sync(FULL_MASK, r0.z, s), __shfl_sync(FULL_MASK, r0.w, s)};
+            const uint4 q1{__shfl_sync(FULL_MASK, r1.x, s), __shfl_sync(FULL_MASK, r1.y, s),
+                           __shfl_sync(FULL_MASK, r1.z, s), __shfl_sync(FULL_MASK, r1.w, s)};
+            ok = piece_advance(rv, n, g + s, q0, q1, sb, stage, lane);
+            pos = s + 1;
+        }
+    }
+    return ok ? __uint_as_float(sb) : warp_plain_sum(rv, n, lane);
+}
 
 template<bool NODIV>
-__global__ void __launch_bounds__(LONG_SUM_THREADS) k_pr_long_sums(PrArgs a, uint32_t *ctr)
+__global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr_long_sums(PrArgs a, uint32_t *ctr)
 {
-    __shared__ float stage[LONG_SUM_THREADS / 32][33 * TERMS_PER_LANE];
+    __shared__ __align__(16) float stage[LONG_SUM_THREADS / 32][33 * PIECE_L];
     resolve_args(a);
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t L = *a.long_total, G = *a.giant_total;
-    const uint32_t jobs = G + (L - G + 31) / 32;
+    const uint32_t L = *a.long_total, G = *a.giant_total, PG = *a.giant_pieces;
+    const uint32_t MB = (L - G + 31) / 32, jobs = MB + PG;
     const float base_nd = nodiv_base(a.n);
     float dsum = 0.0f;
     for (;;) {
@@ -985,19 +1273,40 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS) k_pr_long_sums(PrArgs a, uin
         if (lane == 0) job = atomicAdd(&ctr[0], 1u);
         job = __shfl_sync(FULL_MASK, job, 0);
         if (job >= jobs) break;
-        if (job < G) {
-            const uint32_t row = a.long_rows[job];
-            const uint32_t beg = a.rev_v[row], len = a.rev_v[row + 1] - beg;
-            const float total = warp_sequential_sum<TERMS_PER_LANE>(a.vals + beg, len, stage[wib], lane);
-            if (lane == 0) dsum += finish_vertex<NODIV>(a, row, total, base_nd);
-        } else {
-            const uint32_t k = G + (job - G) * 32 + lane;
+        if (job < MB) {
+            const uint32_t k = G + job * 32 + lane;
             if (k < L) {
                 const uint32_t row = a.long_rows[k];
                 const FinishIn fin = finish_load<NODIV>(a, row);
                 const uint32_t beg = a.rev_v[row];
                 const float sum = lane_sequential_sum(a.vals + beg, a.rev_v[row + 1] - beg);
                 dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
+            }
+        } else {
+            job -= MB;
+            const uint4 w = a.work[job];
+            const uint32_t row = w.x, beg = a.rev_v[row], n = a.rev_v[row + 1] - beg;
+            const uint32_t q = (w.z - beg) / SEG_EDGES, pieces = (n + SEG_EDGES - 1) / SEG_EDGES, p0 = job - q;
+            const float *rv = a.vals + beg;
+            uint4 r0 = make_uint4(REC_NONE, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
+            if (q == 0) {
+                r0 = make_uint4(REC_STATE, warp_serial_start(rv, stage[wib], lane), 0u, 0u);
+            } else if (q >= SERIAL_PIECES) {
+                piece_record(a, rv, n, p0, q, stage[wib], lane, r0, r1);
+            }
+            uint32_t last = 0;
+            if (lane == 0) {
+                a.piece_map[2 * static_cast<uint64_t>(job)] = r0;
+                a.piece_map[2 * static_cast<uint64_t>(job) + 1] = r1;
+                last = atomic_add_acq_rel(&a.long_count[row], 1u) + 1 == pieces ? 1u : 0u;
+            }
+            if (__shfl_sync(FULL_MASK, last, 0)) {
+                __syncwarp();                         // orders every lane's reads after lane 0's acquire
+                const float total = combine_pieces(a, rv, n, p0, pieces, stage[wib], lane);
+                if (lane == 0) {
+                    dsum += finish_vertex<NODIV>(a, row, total, base_nd);
+                    a.long_count[row] = 0;
+                }
             }
         }
     }
@@ -1043,6 +1352,9 @@ struct PrRun {
     uint32_t *long_rows = nullptr;     // long rows by decreasing length
     uint32_t *long_total = nullptr;    // device: number of long rows
     uint32_t *giant_total = nullptr;   // device: how many of them exceed GIANT_ROW
+    uint32_t *giant_pieces = nullptr;  // device: the pieces of those
+    float *piece_sum = nullptr;        // exact pieces: their float sums
+    uint4 *piece_map = nullptr;        // giant-row pieces: records (two uint4 each)
     uint32_t *sum_ctr = nullptr;       // k_pr_long_sums' job and finish counters
     const uint32_t *count_all = nullptr;       // device: items in the list
     const uint32_t *count_nonconst = nullptr;  // device: items before the CONST ones
@@ -1166,7 +1478,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     const uint64_t o_ppos = at; at += al(lcap + 1);
     const uint64_t o_wcnt = at; at += al(2 * windows + 1);
     const uint64_t o_first = at; at += al(2 * windows + 1);
-    const uint64_t o_tot = at; at += al(5);
+    const uint64_t o_tot = at; at += al(6);
     const uint64_t o_temp = at;
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.scratch), o_temp * sizeof(uint32_t) + temp, s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
@@ -1179,6 +1491,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     run.long_total = lpos + n;
     run.giant_total = tot + 2;
     run.sum_ctr = tot + 3;
+    run.giant_pieces = tot + 5;
     const unsigned grid = ctx->sm_count * 4;
     // 1. row classes and the partition
     k_row_flags<<<grid, 256, 0, s>>>(g->rev_vertices, n, flag, lflag);
@@ -1197,7 +1510,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     BW_CUDA(cudaMemsetAsync(pcnt + lcap, 0, sizeof(uint32_t), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
-                                      split, run.work, run.long_count, run.giant_total);
+                                      split, run.work, run.long_count, run.giant_total, run.giant_pieces);
     BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
     k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, wcnt);
@@ -1208,8 +1521,12 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     BW_CUDA(cudaGetLastError());
     run.count_nonconst = tot;
     run.count_all = tot + 1;
-    if (!split && m)
+    if (!split && m) {
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
+        const uint64_t pcap = m / SEG_EDGES + lcap + 1;     // pieces at most
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_map), 2 * pcap * sizeof(uint4), s));
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_sum), pcap * sizeof(float), s));
+    }
     return BW_OK;
 }
 
@@ -1219,6 +1536,8 @@ void free_run(PrRun &run, cudaStream_t s)
     if (run.long_count) cudaFreeAsync(run.long_count, s);
     if (run.scratch) cudaFreeAsync(run.scratch, s);
     if (run.vals) cudaFreeAsync(run.vals, s);
+    if (run.piece_map) cudaFreeAsync(run.piece_map, s);
+    if (run.piece_sum) cudaFreeAsync(run.piece_sum, s);
     if (run.rows) cudaFreeAsync(run.rows, s);
     run = PrRun{};
 }
@@ -1235,13 +1554,13 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_VERTEX_PULL:
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        k_pr_long_sums<false><<<ctx->sm_count * 4, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_NODIV:
         if (geo.block == PULL_WIDE) k_pr_pull_items<true, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<true, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        k_pr_long_sums<true><<<ctx->sm_count * 4, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        k_pr_long_sums<true><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_WARP: k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
@@ -1464,6 +1783,9 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.long_rows = items.long_rows;
         a.long_total = items.long_total;
         a.giant_total = items.giant_total;
+        a.giant_pieces = items.giant_pieces;
+        a.piece_sum = items.piece_sum;
+        a.piece_map = items.piece_map;
         a.sum_ctr = items.sum_ctr;
         // div: rows without in-edges hold the same rank and contribution in
         // both buffers once iterations 1 and 2 have written them

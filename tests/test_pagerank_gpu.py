@@ -67,11 +67,13 @@ def test_variant_parity(ctx, graphs, variant, iterations):
 
 def _chosen_in_degrees(n=80000, seed=9):
     """In-rows of chosen lengths around every boundary of the long-row paths
-    (pieces of 512, batches of rows up to 4096 terms, whole-warp rows above
-    it), sources drawn at random with varied out-degrees."""
+    (pieces of 512, batches of rows up to 2048 terms, piece-parallel rows
+    above it, their 1024-term serial start), sources drawn at random with
+    varied out-degrees."""
     rng = np.random.default_rng(seed)
-    lengths = [1, 255, 256, 257, 300, 511, 512, 513, 1023, 1024, 1025, 4095, 4096, 4097, 5000, 20000]
-    lengths += list(rng.integers(257, 4096, 70))
+    lengths = [1, 255, 256, 257, 300, 511, 512, 513, 1023, 1024, 1025, 1535, 1536, 1537, 2047, 2048, 2049,
+               2560, 2561, 4095, 4096, 4097, 5000, 20000]
+    lengths += list(rng.integers(257, 6000, 70))
     src, dst = [], []
     for v, d in enumerate(lengths):
         src.append(rng.choice(np.arange(len(lengths), n), size=d, replace=False))
@@ -95,8 +97,8 @@ def long_graphs(ctx):
 @pytest.mark.parametrize("iterations", [1, 2, 30])
 def test_long_rows(ctx, long_graphs, variant, iterations):
     """In-rows far longer than one work item, on every path the exact
-    variants take (batches of rows up to 4096 terms summed one row per lane,
-    longer rows summed by a whole warp), including a 199,999-term row of
+    variants take (batches of rows up to 2048 terms summed one row per lane,
+    longer rows summed piece-parallel), including a 199,999-term row of
     equal terms (a round-half-even tie at nearly every step), rows at every
     length boundary and R-MAT hubs: bit-identical to the reference.  The
     reference's own loop can be far from FP64 on such rows (1.2e-3 after one

@@ -41,11 +41,12 @@ static uint32_t sequential(const std::vector<float> &x) {
 static uint32_t serial_terms = 0;
 static uint32_t L = 8;
 
-// Warp emulation; returns false when the kernel would fall back.
-static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
-    const uint32_t WIN = 32 * L, n = vals.size();
-    uint32_t sb = 0;
-    for (uint32_t w = 0; w < n; w += WIN) {
+// Warp emulation of the continuation over terms [b, e) from the running sum
+// sb (warp_sequential_continue); returns false when the kernel would fall
+// back.
+static bool warp_continue(const std::vector<float> &vals, uint32_t b, uint32_t e, uint32_t &sb) {
+    const uint32_t WIN = 32 * L, n = e;
+    for (uint32_t w = b; w < n; w += WIN) {
         uint32_t pos = 0;
         if (w < serial_terms) {            // terms [w, serial_terms) in order by one lane
             volatile float acc = bf(sb);
@@ -139,6 +140,12 @@ static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
             if (exponent_of(sb) == 0xffu) return false;
         }
     }
+    return true;
+}
+
+static bool warp_sum(const std::vector<float> &vals, uint32_t &out) {
+    uint32_t sb = 0;
+    if (!warp_continue(vals, 0, vals.size(), sb)) return false;
     out = sb;
     return true;
 }
@@ -147,10 +154,110 @@ static uint64_t rng = 0x243f6a8885a308d3ULL;
 static uint64_t nxt() { rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17; return rng; }
 static double unit() { return (nxt() >> 11) * (1.0 / 9007199254740992.0); }
 
+// Piece-parallel emulation (the giant rows of k_pr_long_sums): pieces of
+// 512 terms; piece 0 adds the first 1024 terms in order; every later piece
+// guesses the running sum at its start (the float sums of the pieces before
+// it, added in double) and records, in the guessed binade, the map of its
+// terms, or -- when the guessed sum crosses into the next binade inside the
+// piece -- the map before the crossing term, that term, and the map of the
+// rest in the new binade.  The combination applies a record where it holds
+// for the true running sum and evaluates the piece exactly otherwise.
+// guess_mode 1 replaces the guesses by wrong ones (a neighbouring binade,
+// a shifted significand, or none) at random: the result must not change.
+static int guess_mode = 0;
+static long pieces_mapped = 0, pieces_crossed = 0, pieces_exact = 0;
+struct Rec { uint32_t kind = 0, K = 0, K2 = 0, tg = 0, xb = 0; Map m1{0, 0}, m2{0, 0}; };
+
+static Rec make_record(const std::vector<float> &vals, uint32_t b, uint32_t e, uint32_t guess) {
+    Rec r;
+    if (!in_domain(guess)) return r;
+    const uint32_t K = exponent_of(guess);
+    bool good = true;
+    Map total = identity();
+    for (uint32_t i = b; i < e; i++) total = compose(total, step_select(fb(vals[i]), K, good));
+    if (!good) return r;
+    uint32_t acc = significand_of(guess), nb = 0;
+    int tg = -1;
+    Map m1 = identity();
+    for (uint32_t i = b; i < e && tg < 0; i++) {
+        Map st; step(fb(vals[i]), K, st);
+        const uint32_t bu = apply(st, acc);
+        if (bu >= TOP) {
+            tg = static_cast<int>(i - b);
+            volatile float s0 = bf(bits_of(K, acc));
+            volatile float s1 = s0 + vals[i];
+            nb = fb(s1);
+        } else { acc = bu; m1 = compose(m1, st); }
+    }
+    if (tg < 0) { r.kind = 1; r.K = K; r.m1 = total; return r; }
+    if (!in_domain(nb)) return r;
+    const uint32_t K2 = exponent_of(nb);
+    Map m2 = identity();
+    for (uint32_t i = b + tg + 1; i < e; i++) m2 = compose(m2, step_select(fb(vals[i]), K2, good));
+    r.kind = 3; r.K = K; r.K2 = K2; r.tg = tg; r.xb = fb(vals[b + tg]); r.m1 = m1; r.m2 = m2;
+    return r;
+}
+
+static bool piece_advance(const std::vector<float> &vals, uint32_t b, uint32_t e, const Rec &r, uint32_t &sb) {
+    if ((r.kind == 1 || r.kind == 3) && in_domain(sb) && exponent_of(sb) == r.K) {
+        const uint32_t a1 = apply(r.m1, significand_of(sb));
+        if (r.kind == 1 && a1 < TOP) { sb = bits_of(r.K, a1); pieces_mapped++; return true; }
+        Map st;
+        if (r.kind == 3 && a1 < TOP && step(r.xb, r.K, st) && apply(st, a1) >= TOP) {
+            volatile float s0 = bf(bits_of(r.K, a1));
+            volatile float s1 = s0 + bf(r.xb);
+            const uint32_t nb = fb(s1);
+            if (in_domain(nb) && exponent_of(nb) == r.K2) {
+                const uint32_t a3 = apply(r.m2, significand_of(nb));
+                if (a3 < TOP) { sb = bits_of(r.K2, a3); pieces_crossed++; return true; }
+            }
+        }
+    }
+    pieces_exact++;
+    return warp_continue(vals, b, e, sb);
+}
+
+static bool piece_sum(const std::vector<float> &vals, uint32_t &out) {
+    const uint32_t PIECE = 512, n = vals.size(), P = (n + PIECE - 1) / PIECE;
+    const uint32_t save_l = L, save_st = serial_terms;
+    L = PIECE / 32; serial_terms = 1024;
+    std::vector<float> ps(P);
+    for (uint32_t p = 0; p < P; p++) {              // in any order: here backwards
+        volatile float s = 0.0f;
+        for (uint32_t i = std::min(n, (p + 1) * PIECE); i-- > p * PIECE;) s = s + vals[i];
+        ps[p] = s;
+    }
+    std::vector<Rec> rec(P);
+    for (uint32_t q = 2; q < P; q++) {
+        double pre = 0.0;
+        for (uint32_t i = 0; i < q; i++) pre += ps[i];
+        uint32_t g = fb(static_cast<float>(pre));
+        if (guess_mode == 1) {
+            const uint32_t r = nxt() % 5;
+            if (r == 1 && exponent_of(g) > 1) g -= 1u << 23;
+            if (r == 2 && exponent_of(g) < 0xfdu) g += 1u << 23;
+            if (r == 3) g = 0;
+            if (r == 4) g ^= static_cast<uint32_t>(nxt()) & 0x7fffffu;
+        }
+        rec[q] = make_record(vals, q * PIECE, std::min(n, q * PIECE + PIECE), g);
+    }
+    volatile float s0 = 0.0f;                        // the serial start
+    for (uint32_t i = 0; i < std::min(n, 1024u); i++) s0 = s0 + vals[i];
+    uint32_t sb = fb(s0);
+    bool ok = true;
+    for (uint32_t q = 2; q < P && ok; q++) ok = piece_advance(vals, q * PIECE, std::min(n, q * PIECE + PIECE), rec[q], sb);
+    L = save_l; serial_terms = save_st;
+    if (!ok) return false;
+    out = sb;
+    return true;
+}
+
+
 static int bad = 0, tested = 0, fallback = 0;
+static bool use_pieces = false;
 static void check(const std::vector<float> &x, bool expect_domain) {
     uint32_t got;
-    const bool ok = warp_sum(x, got);
+    const bool ok = use_pieces ? piece_sum(x, got) : warp_sum(x, got);
     tested++;
     if (!ok) {
         fallback++;
@@ -166,9 +273,17 @@ static void check(const std::vector<float> &x, bool expect_domain) {
 
 static void run_all();
 
-int main() {
-    for (uint32_t l : {8u, 32u})
-        for (uint32_t st : {0u, 64u, 300u, 1024u}) { L = l; serial_terms = st; run_all(); }
+static void run_giant();
+
+int main(int argc, char **argv) {
+    if (argc > 1) {                                  // the piece-parallel scheme
+        use_pieces = true;
+        for (int mode : {0, 1}) { guess_mode = mode; run_giant(); }
+        std::printf("mapped %ld crossed %ld exact %ld\n", pieces_mapped, pieces_crossed, pieces_exact);
+    } else {
+        for (uint32_t l : {8u, 32u})
+            for (uint32_t st : {0u, 64u, 300u, 1024u}) { L = l; serial_terms = st; run_all(); }
+    }
     std::printf("tested %d fallback %d bad %d\n", tested, fallback, bad);
     return bad ? 1 : 0;
 }
@@ -244,6 +359,62 @@ static void run_all() {
         std::vector<float> w(600, 3e38f); check(w, false);
     }
 }
+
+// Rows above the giant threshold, as the piece-parallel scheme sees them.
+static void run_giant() {
+    // log-uniform magnitudes
+    for (int t = 0; t < 150; t++) {
+        const uint32_t n = 4097 + nxt() % 60000;
+        const int span = 1 + nxt() % 40;
+        std::vector<float> x(n);
+        for (auto &v : x) v = static_cast<float>(std::ldexp(1.0 + unit(), -static_cast<int>(nxt() % span) - 10));
+        check(x, true);
+    }
+    // equal terms: running sums at exact powers of two, ties at every step
+    for (int t = 0; t < 60; t++) {
+        const uint32_t n = 4097 + nxt() % 200000;
+        const float v = static_cast<float>(std::ldexp(1.0 + (nxt() % 8) / 8.0, -static_cast<int>(nxt() % 30)));
+        std::vector<float> x(n, v);
+        check(x, true);
+    }
+    // PageRank-like terms, hub-sized rows
+    for (int t = 0; t < 60; t++) {
+        const uint32_t n = 4097 + nxt() % 120000;
+        const float base = 1.0f / static_cast<float>(1u << (10 + nxt() % 14));
+        std::vector<float> x(n);
+        for (auto &v : x) v = base / static_cast<float>(1 + nxt() % 64);
+        check(x, true);
+    }
+    // growing magnitudes: a binade crossing in most pieces; and shrinking
+    for (int t = 0; t < 60; t++) {
+        const uint32_t n = 4097 + nxt() % 30000;
+        std::vector<float> x(n);
+        const uint32_t step = n / 100 + 1 + nxt() % 600;   // up to 2^40: no overflow
+        for (uint32_t i = 0; i < n; i++) x[i] = static_cast<float>(std::ldexp(1.0 + unit(), static_cast<int>(i / step) - 60));
+        check(x, true);
+        std::vector<float> y(x.rbegin(), x.rend());
+        check(y, true);
+    }
+    // zeros through the serial start and beyond, then terms
+    for (int t = 0; t < 40; t++) {
+        const uint32_t n = 4097 + nxt() % 20000, lead = nxt() % n;
+        std::vector<float> x(n);
+        for (uint32_t i = 0; i < n; i++) x[i] = i < lead ? 0.0f : static_cast<float>(std::ldexp(1.0 + unit(), -20));
+        check(x, true);
+    }
+    // one huge term late in the row: every later guess is far off
+    for (int t = 0; t < 40; t++) {
+        const uint32_t n = 4097 + nxt() % 20000;
+        std::vector<float> x(n, 1e-6f);
+        x[2048 + nxt() % (n - 2048)] = 1e3f;
+        check(x, true);
+    }
+    // out of domain in a mapped piece: reported
+    {
+        std::vector<float> x(9000, 1.0f); x[7000] = -1.0f; check(x, false);
+        std::vector<float> y(9000, 1.0f); y[5000] = 1e-40f; check(y, false);
+    }
+}
 """
 
 
@@ -256,6 +427,26 @@ def test_warp_sequential_sum_matches_loop(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stdout[-3000:]
     assert "bad 0" in out.stdout
+
+
+def test_piece_parallel_sum_matches_loop(tmp_path):
+    """The giant-row scheme of k_pr_long_sums (per 512-term piece, maps in a
+    guessed binade with the guessed crossing term, combined in order with
+    exact re-evaluation where a record does not hold) equals the plain loop
+    bit for bit, with the real guesses and with guesses made wrong at
+    random."""
+    src = tmp_path / "check.cpp"
+    src.write_text(CHECKER)
+    exe = tmp_path / "check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{HEADER.parent}", str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe), "pieces"], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stdout[-3000:]
+    assert "bad 0" in out.stdout
+    assert "fallback 4 " in out.stdout          # the two out-of-domain rows, in both modes
+    words = out.stdout.split("mapped ")[1].split()
+    mapped, crossed, exact = int(words[0]), int(words[2]), int(words[4])
+    assert mapped > exact and crossed > 0       # the records do the bulk of the work
 
 
 STEP_CHECK = r"""
