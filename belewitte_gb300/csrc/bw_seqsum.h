@@ -92,22 +92,36 @@ BWS_HD bool step(uint32_t xb, uint32_t k, Map &m)
 
 // The same map without branches (selects only), for warps whose lanes take
 // different cases at once; `ok` is cleared for terms outside the domain.
+// Both increments are one rounding of mx / 2^d (mx the term's significand,
+// d = k - kx): to nearest with ties to an even quotient (A even: the sum's
+// new significand is even) or to an odd one (A odd), each an addition and
+// a shift: (mx + half - 1 + lsb(q)) >> d and (mx + half - lsb(q)) >> d.
 BWS_HD Map step_select(uint32_t xb, uint32_t k, bool &ok)
 {
     const uint32_t kx = (xb >> 23) & 0xffu;
-    const bool zero = (xb & 0x7fffffffu) == 0;
-    ok = ok && (zero || !((xb >> 31) || kx == 0 || kx == 0xffu));
+    const bool zero = (xb << 1) == 0u;
+    ok = ok && (zero || xb - 0x00800000u < 0x7f000000u);   // +-0, or positive and normal
     const int32_t d = static_cast<int32_t>(k) - static_cast<int32_t>(kx);
     const uint32_t dd = static_cast<uint32_t>(d < 1 ? 1 : (d > 24 ? 24 : d));
     const uint32_t mx = (xb & 0x7fffffu) | ONE;
-    const uint32_t q = mx >> dd, rem = mx & ((1u << dd) - 1u), half = 1u << (dd - 1u);
-    const uint32_t up = rem > half ? 1u : 0u, tie = rem == half ? 1u : 0u, odd = q & 1u;
-    uint32_t e = q + (up | (tie & odd)), o = q + (up | (tie & (odd ^ 1u)));
+    const uint32_t half = 1u << (dd - 1u), qb = (mx >> dd) & 1u;
+    uint32_t e = (mx + half - 1u + qb) >> dd, o = (mx + half - qb) >> dd;
     const bool big = d <= 0, tiny = d >= 25 || zero;
     e = big ? SAT : (tiny ? 0u : e);
     o = big ? SAT : (tiny ? 0u : o);
     return Map{e, o};
 }
+
+// compose() without saturation, for short runs whose increments cannot
+// overflow (at most 64 maps of at most SAT each); saturate() the result.
+// Any run whose true total reaches SAT still totals at least SAT, so the
+// saturated result equals compose()'s.
+BWS_HD Map compose_short(Map f, Map g)
+{
+    return Map{f.e + ((f.e & 1u) ? g.o : g.e), f.o + ((f.o & 1u) ? g.e : g.o)};
+}
+
+BWS_HD Map saturated(Map m) { return Map{saturate(m.e), saturate(m.o)}; }
 
 BWS_HD uint32_t exponent_of(uint32_t sb) { return (sb >> 23) & 0xffu; }
 BWS_HD uint32_t significand_of(uint32_t sb) { return (sb & 0x7fffffu) | ONE; }

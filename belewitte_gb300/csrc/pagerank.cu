@@ -816,9 +816,9 @@ __device__ __forceinline__ bool warp_sequential_continue(const float *vals, uint
 #pragma unroll
             for (uint32_t st = 1; st < L; st <<= 1) {
 #pragma unroll
-                for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
+                for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose_short(t[u], t[u + st]);
             }
-            const Map m = t[0];
+            const Map m = saturated(t[0]);
             if (__any_sync(FULL_MASK, !good)) { ok = false; break; }
             Map incl = m;
 #pragma unroll
@@ -865,7 +865,7 @@ __device__ __forceinline__ bool warp_sequential_continue(const float *vals, uint
 
 // One lane's plain loop over the row (terms outside the maps' domain);
 // every lane returns the sum.
-__device__ __forceinline__ float warp_plain_sum(const float *vals, uint32_t n, unsigned lane)
+__device__ __noinline__ float warp_plain_sum(const float *vals, uint32_t n, unsigned lane)
 {
     float s = 0.0f;
     if (lane == 0)
@@ -1083,9 +1083,9 @@ __device__ __forceinline__ bwseq::Map lane_maps(const uint32_t (&x)[PIECE_L], ui
 #pragma unroll
     for (uint32_t st = 1; st < PIECE_L; st <<= 1) {
 #pragma unroll
-        for (uint32_t u = 0; u + st < PIECE_L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
+        for (uint32_t u = 0; u + st < PIECE_L; u += 2 * st) t[u] = compose_short(t[u], t[u + st]);
     }
-    return t[0];
+    return saturated(t[0]);
 }
 
 // The record of piece q >= SERIAL_PIECES of a giant row (valid in lane 0).
@@ -1184,6 +1184,17 @@ __device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, u
     r1 = make_uint4(xb, m2.e, m2.o, 0u);
 }
 
+// The exact evaluation of piece q from the running sum `sb` (rare: kept
+// out of line, so that the kernel's frequent paths stay small in the
+// instruction cache).  Returns {ok, new sb}.
+__device__ __noinline__ uint2 piece_exact(const float *rv, uint32_t n, uint32_t q, uint32_t sb, float *stage,
+                                          unsigned lane)
+{
+    const uint32_t b = q * SEG_EDGES;
+    const bool ok = warp_sequential_continue<PIECE_L>(rv, b, min(n, b + SEG_EDGES), sb, stage, lane);
+    return make_uint2(ok ? 1u : 0u, sb);
+}
+
 // Piece q from the running sum `sb`: its record when it holds for that sum,
 // else the exact evaluation of its terms.  False when a term or the sum
 // leaves the maps' domain.
@@ -1211,8 +1222,9 @@ __device__ __forceinline__ bool piece_advance(const float *rv, uint32_t n, uint3
             }
         }
     }
-    const uint32_t b = q * SEG_EDGES;
-    return warp_sequential_continue<PIECE_L>(rv, b, min(n, b + SEG_EDGES), sb, stage, lane);
+    const uint2 r = piece_exact(rv, n, q, sb, stage, lane);
+    sb = r.y;
+    return r.x != 0;
 }
 
 // The row's sum from the records of its pieces p0 .. p0 + pieces - 1 (the

@@ -91,8 +91,8 @@ static bool warp_continue(const std::vector<float> &vals, uint32_t b, uint32_t e
                     }
                     if (!good) return false;
                     for (uint32_t st = 1; st < L; st <<= 1)
-                        for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose(t[u], t[u + st]);
-                    m[lane] = t[0];
+                        for (uint32_t u = 0; u + st < L; u += 2 * st) t[u] = compose_short(t[u], t[u + st]);
+                    m[lane] = saturated(t[0]);
                     continue;
                 }
                 m[lane] = identity();
