@@ -145,7 +145,7 @@ def _measured_peak():
 
 # The PageRank variant the headline is measured with: the fastest on this
 # workload in the on-device sweep of every variant (pull-segmented ~249 us,
-# rev-edge-list ~294 us, vertex-pull ~512 us per iteration on R-MAT-22);
+# rev-edge-list ~294 us, vertex-pull ~342 us per iteration on R-MAT-22);
 # --variant measures another one.
 HEADLINE_VARIANT = "pull-segmented"
 
