@@ -445,6 +445,49 @@ def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int =
                        kernel_launches=res.kernel_launches)
 
 
+def gather_ceiling(ctx: Context, src, idx, *, warmup: int = 3, repeats: int = 10, stream=None) -> float:
+    """Scattered 4-byte loads per second that the device sustains: the time
+    of bw_gather_probe gathering src[idx] (float32 and uint32/int32 device
+    tensors), timed with CUDA events on `stream` after `warmup` launches,
+    median of `repeats`.  The bound of the PageRank pull kernels when their
+    gathered vector fits in L2."""
+    torch = _torch()
+    lib = library()
+    st = stream or torch.cuda.current_stream(src.device)
+    partial = torch.empty(ctx.sm_count, dtype=torch.float32, device=src.device)
+
+    def launch():
+        check(lib.bw_gather_probe(ctx.handle, C.c_void_p(_ptr(src)), src.numel(), C.c_void_p(_ptr(idx)),
+                                  idx.numel(), C.c_void_p(_ptr(partial)), C.c_void_p(st.cuda_stream)),
+              "bw_gather_probe")
+
+    for _ in range(warmup):
+        launch()
+    times = []
+    for _ in range(repeats):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        launch()
+        b.record(st)
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    return idx.numel() / float(np.median(times))
+
+
+def gather_probe_sum(ctx: Context, src, idx, stream=None) -> float:
+    """The probe's total (sum of the gathered values, in any order)."""
+    torch = _torch()
+    lib = library()
+    st = stream or torch.cuda.current_stream(src.device)
+    partial = torch.zeros(ctx.sm_count, dtype=torch.float32, device=src.device)
+    check(lib.bw_gather_probe(ctx.handle, C.c_void_p(_ptr(src)), src.numel(), C.c_void_p(_ptr(idx)),
+                              idx.numel(), C.c_void_p(_ptr(partial)), C.c_void_p(st.cuda_stream)),
+          "bw_gather_probe")
+    st.synchronize()
+    return float(partial.double().sum().item())
+
+
 def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], iterations: int = 30,
                       *, ranks=None, time_iterations: bool = False, block: int = 0, grid: int = 0,
                       warp: int = 0, chunk: int = 0, relabel: bool | None = None, stream=None) -> PageRankRun:

@@ -145,6 +145,8 @@ SIGNATURES = {
     "bw_batch_run": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_int, C.c_void_p, C.c_uint32, C.c_void_p,
                                C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                C.POINTER(LaunchConfig), C.POINTER(BatchResult), C.c_void_p]),
+    "bw_gather_probe": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p,
+                                  C.c_void_p]),
     "bw_bfs_run_noalloc": (C.c_int, [C.POINTER(GraphView), C.c_uint32, C.c_void_p, C.c_uint32,
                                      C.POINTER(C.c_uint32), C.c_void_p]),
 }

@@ -700,7 +700,10 @@ __device__ __forceinline__ float lane_sequential_sum(const float *p, uint32_t le
 // among the first `hubs` entries, else from global memory.
 __device__ __forceinline__ float gather1(const float *__restrict__ src, const float *hub, uint32_t hubs, uint32_t i)
 {
-    return i < hubs ? hub[i] : __ldg(src + i);
+    // L2 only: random lines would only evict one another from L1 (measured
+    // on GB300: ER(4M, 67M) 278 -> 268 us per iteration; reading the next
+    // tier of hubs through L1 instead gained nothing on R-MAT-22)
+    return i < hubs ? hub[i] : __ldcg(src + i);
 }
 
 // Gather src[rev_e[e0 + k]] for k in [0, len) (len <= SEG_EDGES) into buf.

@@ -18,6 +18,9 @@ The same JSON line carries:
     sources, each in one persistent launch.
   * roofline of the dominant PageRank kernel, e2e through the C ABI with
     host buffers, the CPU baseline, clocks during the timed region.
+  * gather_roofline: the PageRank iteration's gathers per second against the
+    device's ceiling for scattered 4-byte loads, measured in the same run by
+    the library's probe kernel (M uniform random gathers over N).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --case pagerank:VARIANT:rmat22|er[:BLOCK:HUBS]   (small profiling case)
@@ -348,6 +351,16 @@ def run_ours(args):
     ab = alg_bytes(variant, n, m)
     peak, peak_kind = _measured_peak()
     achieved = ab / (kernel_ms * 1e-3) / 1e9
+    # The gathered vector (4N bytes) fits in L2: the pull kernels are bound
+    # by scattered 4-byte loads, not by HBM.  Their ceiling on this device:
+    # M uniform random gathers over N entries by the probe kernel.
+    gen = torch.Generator(device=f"cuda:{dev}")
+    gen.manual_seed(SEED)
+    probe_idx = torch.randint(0, n, (m,), dtype=torch.int32, device=f"cuda:{dev}", generator=gen)
+    probe_src = torch.rand(n, dtype=torch.float32, device=f"cuda:{dev}", generator=gen)
+    ceiling = bw.gather_ceiling(ctx, probe_src, probe_idx)
+    del probe_idx, probe_src
+    gathers = m / (kernel_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ----------------------
     host = g.to_host_arrays()
@@ -393,6 +406,10 @@ def run_ours(args):
                      "frac": round(achieved / peak, 4), "traffic": _profiled_traffic(variant),
                      "kernel": DOMINANT.get(variant, "k_pr_edge"), "kernel_ms": round(kernel_ms, 5),
                      "algorithmic_bytes": ab, "peak_source": peak_kind},
+        "gather_roofline": {"bound": "scattered 4-byte loads", "achieved": round(gathers / 1e9, 1),
+                            "peak": round(ceiling / 1e9, 1), "unit": "Ggathers/s",
+                            "frac": round(gathers / ceiling, 4),
+                            "peak_source": "bw_gather_probe: M uniform random gathers over N, measured in this run"},
         "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n * 4)},
         "gpu_launches": launches,

@@ -540,6 +540,20 @@ int bw_bfs_run_noalloc(const bw_graph_view *g, uint32_t root, int32_t *levels,
                        uint32_t max_levels, uint32_t *level_count,
                        void *stream);
 
+/*
+ * Random-gather ceiling (a measurement; no counterpart in the reference):
+ * partial[b] = sum over the loads block b issued of src[idx[i]], i < m,
+ * skipping idx[i] >= n.  One block per SM (partial holds
+ * bw_context_sm_count(ctx) floats), 16 independent loads in flight per
+ * thread, L2-only loads -- the gathers of the PageRank pull kernels with
+ * nothing else to do.  Time it on `stream` to get the device's rate of
+ * scattered 4-byte loads, the bound of those kernels when their gathered
+ * vector fits in L2.
+ */
+int bw_gather_probe(bw_context *ctx, const float *src, uint64_t n,
+                    const uint32_t *idx, uint64_t m, float *partial,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

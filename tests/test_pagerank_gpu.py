@@ -202,3 +202,18 @@ def test_reverse_only_view(ctx, graphs, long_graphs, variant):
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name)
         elif _rel(ref, r64) <= REL_REF:
             assert _rel(got, ref) <= REL_REF, (variant, name)
+
+
+def test_gather_probe(ctx):
+    """bw_gather_probe sums exactly the gathered values (indices past the
+    array skipped) and reports a positive rate."""
+    torch = pytest.importorskip("torch")
+    gen = torch.Generator(device="cuda:0")
+    gen.manual_seed(5)
+    n, m = 1 << 20, 3_000_001
+    src = torch.randint(0, 8, (n,), dtype=torch.int32, device="cuda:0", generator=gen).float()
+    idx = torch.randint(0, n + 1000, (m,), dtype=torch.int32, device="cuda:0", generator=gen)
+    ok = idx < n
+    want = float(src[idx[ok].long()].double().sum().item())
+    assert bw.gather_probe_sum(ctx, src, idx) == want         # small integers: exact in any order
+    assert bw.gather_ceiling(ctx, src, idx, warmup=1, repeats=3) > 1e9
