@@ -195,8 +195,37 @@ __global__ void __launch_bounds__(512) k_bfs_edge(BfsArgs a)
 
 // ---------------------------------------------------------------------------
 // vertex-push (bfs/vertex_push.cu:3-26): thread per vertex; a frontier
-// vertex's owner walks its CSR row.  Depths are scanned 4 per thread.
+// vertex's owner walks its CSR row.  Depths are scanned 4 per thread.  A
+// row longer than BFS_PUSH_HEAVY is expanded by the owner's whole warp
+// (lane-strided, coalesced) instead of by its one thread, whose serial
+// chain of relaxations would otherwise hold the level: a hub's row is the
+// level's critical path.
 // ---------------------------------------------------------------------------
+constexpr uint32_t BFS_PUSH_HEAVY = 32;
+constexpr int BFS_PUSH_UNROLL = 8;
+
+// Relaxes the neighbours E[first + k * step] (k < BFS_PUSH_UNROLL, below
+// `end`): their indices, then their depths, are all in flight before the
+// relaxations, and only a neighbour not yet visited costs an atomic.
+template<int RED, bool SIDE>
+__device__ __forceinline__ void relax_neighbours(const BfsArgs &a, const uint32_t *E, int32_t *lv, int32_t nd,
+                                                 uint32_t first, uint32_t step, uint32_t end, Counter<RED> &cnt,
+                                                 Side<SIDE> &side, uint32_t *qnext, LevelSlot *slot)
+{
+    uint32_t u[BFS_PUSH_UNROLL];
+    int32_t d[BFS_PUSH_UNROLL];
+#pragma unroll
+    for (int k = 0; k < BFS_PUSH_UNROLL; k++) {
+        const uint32_t i = first + k * step;
+        u[k] = i < end ? __ldg(E + i) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < BFS_PUSH_UNROLL; k++) d[k] = first + k * step < end ? lv[u[k]] : nd;
+#pragma unroll
+    for (int k = 0; k < BFS_PUSH_UNROLL; k++)
+        if (d[k] > nd && atomicMin(&lv[u[k]], nd) > nd) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, u[k]); }
+}
+
 template<int RED, bool SIDE>
 __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
 {
@@ -207,24 +236,48 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
     int32_t *lv = a.levels;
     Counter<RED> cnt;
     Side<SIDE> side;
+    const unsigned lane = threadIdx.x & 31;
     const uint64_t n = a.n, stride = gthreads();
-    auto expand = [&](uint64_t v) {
-        const uint32_t s = a.fwd_v[v], e = a.fwd_v[v + 1];
-        for (uint32_t i = s; i < e; i++) {
-            const uint32_t u = __ldg(a.fwd_e + i);
-            if (relax(lv, u, nd)) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, u); }
+    // every lane calls it (warp-uniform loops); rows [s, e) of frontier
+    // vertices, empty for the others
+    auto relax_batch = [&](uint32_t first, uint32_t step, uint32_t end) {
+        relax_neighbours(a, a.fwd_e, lv, nd, first, step, end, cnt, side, qnext, slot);
+    };
+    auto expand = [&](uint32_t s, uint32_t e) {
+        const bool heavy = e - s > BFS_PUSH_HEAVY;
+        if (!heavy)
+            for (uint32_t i = s; i < e; i += BFS_PUSH_UNROLL) relax_batch(i, 1, e);
+        for (unsigned hv = __ballot_sync(FULL_MASK, heavy); hv; hv &= hv - 1) {
+            const unsigned l = __ffs(hv) - 1;
+            const uint32_t hs = __shfl_sync(FULL_MASK, s, l), he = __shfl_sync(FULL_MASK, e, l);
+            for (uint32_t base = hs; base < he; base += 32 * BFS_PUSH_UNROLL) relax_batch(base + lane, 32, he);
         }
     };
     const uint64_t groups = (reinterpret_cast<uintptr_t>(lv) & 15) ? 0 : n >> 2;
-    for (uint64_t g = gtid(); g < groups; g += stride) {
-        const int4 l = reinterpret_cast<const int4 *>(lv)[g];
-        if (l.x == depth) expand(4 * g);
-        if (l.y == depth) expand(4 * g + 1);
-        if (l.z == depth) expand(4 * g + 2);
-        if (l.w == depth) expand(4 * g + 3);
+    for (uint64_t g0 = gtid() - lane; g0 < groups; g0 += stride) {
+        const uint64_t g = g0 + lane;
+        int4 l = make_int4(-1, -1, -1, -1);
+        if (g < groups) l = reinterpret_cast<const int4 *>(lv)[g];
+        const int32_t d4[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t s = 0, e = 0;
+            if (d4[k] == depth) {
+                s = a.fwd_v[4 * g + k];
+                e = a.fwd_v[4 * g + k + 1];
+            }
+            expand(s, e);
+        }
     }
-    for (uint64_t v = (groups << 2) + gtid(); v < n; v += stride)
-        if (lv[v] == depth) expand(v);
+    for (uint64_t v0 = (groups << 2) + gtid() - lane; v0 < n; v0 += stride) {
+        const uint64_t v = v0 + lane;
+        uint32_t s = 0, e = 0;
+        if (v < n && lv[v] == depth) {
+            s = a.fwd_v[v];
+            e = a.fwd_v[v + 1];
+        }
+        expand(s, e);
+    }
     cnt.finish(&slot->frontier);
     side.finish(slot);
 }
@@ -232,7 +285,13 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
 // ---------------------------------------------------------------------------
 // vertex-pull (bfs/vertex_pull.cu:3-31): thread per vertex; an unvisited
 // vertex scans its reverse row and stops at the first parent at `depth`.
+// The row is scanned BFS_PULL_UNROLL edges at a time: their indices, then
+// their depths, are in flight together (a chain of dependent loads per
+// edge would otherwise bound the thread); the few loads past the first
+// parent are the price of the early exit.
 // ---------------------------------------------------------------------------
+constexpr int BFS_PULL_UNROLL = 4;
+
 template<int RED, bool SIDE>
 __global__ void __launch_bounds__(512) k_bfs_vertex_pull(BfsArgs a)
 {
@@ -244,27 +303,23 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_pull(BfsArgs a)
     Counter<RED> cnt;
     Side<SIDE> side;
     const uint64_t n = a.n, stride = gthreads();
-    auto pull = [&](uint64_t v) {
+    for (uint64_t v = gtid(); v < n; v += stride) {
+        if (lv[v] <= nd) continue;
         const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
-        for (uint32_t i = s; i < e; i++) {
-            if (lv[__ldg(a.rev_e + i)] == depth) {
-                lv[v] = nd;
-                cnt.hit(&slot->frontier);
-                side.visit(a, qnext, slot, static_cast<uint32_t>(v));
-                break;
-            }
+        bool found = false;
+        for (uint32_t i = s; i < e && !found; i += BFS_PULL_UNROLL) {
+            uint32_t p[BFS_PULL_UNROLL];
+#pragma unroll
+            for (int k = 0; k < BFS_PULL_UNROLL; k++) p[k] = i + k < e ? __ldg(a.rev_e + i + k) : 0u;
+#pragma unroll
+            for (int k = 0; k < BFS_PULL_UNROLL; k++) found |= i + k < e && lv[p[k]] == depth;
         }
-    };
-    const uint64_t groups = (reinterpret_cast<uintptr_t>(lv) & 15) ? 0 : n >> 2;
-    for (uint64_t g = gtid(); g < groups; g += stride) {
-        const int4 l = reinterpret_cast<const int4 *>(lv)[g];
-        if (l.x > nd) pull(4 * g);
-        if (l.y > nd) pull(4 * g + 1);
-        if (l.z > nd) pull(4 * g + 2);
-        if (l.w > nd) pull(4 * g + 3);
+        if (found) {
+            lv[v] = nd;
+            cnt.hit(&slot->frontier);
+            side.visit(a, qnext, slot, static_cast<uint32_t>(v));
+        }
     }
-    for (uint64_t v = (groups << 2) + gtid(); v < n; v += stride)
-        if (lv[v] > nd) pull(v);
     cnt.finish(&slot->frontier);
     side.finish(slot);
 }
@@ -317,12 +372,9 @@ __global__ void __launch_bounds__(512) k_bfs_vwarp(BfsArgs a)
         for (uint32_t v = 0; v < cntv; v++) {
             const uint32_t s = my_off[v], e = my_off[v + 1];
             if constexpr (!PULL) {
-                if (my_lv[v] == depth) {
-                    for (uint32_t i = s + lane; i < e; i += W) {
-                        const uint32_t u = __ldg(E + i);
-                        if (relax(lv, u, nd)) { cnt.hit(&slot->frontier); side.visit(a, qnext, slot, u); }
-                    }
-                }
+                if (my_lv[v] == depth)
+                    for (uint32_t base = s; base < e; base += W * BFS_PUSH_UNROLL)
+                        relax_neighbours(a, E, lv, nd, base + lane, W, e, cnt, side, qnext, slot);
             } else {
                 if (my_lv[v] > depth) {
                     bool found = false;

@@ -339,19 +339,54 @@ __global__ void __launch_bounds__(256) k_pr_edge(PrArgs a)
 
 // ----------------------------- vertex-push --------------------------------
 // Thread per vertex; each owner scatters pr[v] / rowlen to its out-row
-// (pagerank/vertex_push.cu:3-31).
+// (pagerank/vertex_push.cu:3-31).  Rows longer than PUSH_HEAVY would keep
+// one lane issuing its row's atomics one after the other while the rest of
+// its warp idles: the warp expands those rows together instead (coalesced
+// index loads, one row after the other, in lane order).
+constexpr uint32_t PUSH_HEAVY = 32;
+constexpr int PUSH_UNROLL = 8;
+
 __global__ void __launch_bounds__(256) k_pr_vertex_push(PrArgs a)
 {
-    for (uint64_t v = gtid(); v < a.n; v += gthreads()) {
-        const uint32_t s = a.fwd_v[v], e = a.fwd_v[v + 1];
-        if (s == e) continue;
-        const float out = a.contrib_in[v];
-        for (uint32_t i = s; i < e; i++) atomicAdd(&a.acc[__ldg(a.fwd_e + i)], out);
+    const unsigned lane = threadIdx.x & 31;
+    for (uint64_t w0 = gtid() - lane; w0 < a.n; w0 += gthreads()) {
+        const uint64_t v = w0 + lane;
+        uint32_t s = 0, e = 0;
+        if (v < a.n) {
+            s = a.fwd_v[v];
+            e = a.fwd_v[v + 1];
+        }
+        const float out = s < e ? a.contrib_in[v] : 0.0f;
+        const bool heavy = e - s > PUSH_HEAVY;
+        if (!heavy) {
+#pragma unroll 4
+            for (uint32_t i = s; i < e; i++) atomicAdd(&a.acc[__ldg(a.fwd_e + i)], out);
+        }
+        for (unsigned hv = __ballot_sync(FULL_MASK, heavy); hv; hv &= hv - 1) {
+            const unsigned l = __ffs(hv) - 1;
+            const uint32_t hs = __shfl_sync(FULL_MASK, s, l), he = __shfl_sync(FULL_MASK, e, l);
+            const float ho = __shfl_sync(FULL_MASK, out, l);
+            for (uint32_t base = hs; base < he; base += 32 * PUSH_UNROLL) {
+                uint32_t d[PUSH_UNROLL];
+#pragma unroll
+                for (int u = 0; u < PUSH_UNROLL; u++) {
+                    const uint32_t i = base + u * 32 + lane;
+                    d[u] = i < he ? __ldcs(a.fwd_e + i) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < PUSH_UNROLL; u++)
+                    if (base + u * 32 + lane < he) atomicAdd(&a.acc[d[u]], ho);
+            }
+        }
     }
 }
 
-// vertex-push-warp (pagerank/vertex_push_warp.cu:4-49): virtual warp of W
-// lanes per chunk of C vertices, ranks and offsets staged in shared memory.
+// vertex-push-warp (pagerank/vertex_push_warp.cu:4-49): a virtual warp of W
+// lanes per chunk of C vertices, contributions and offsets staged in shared
+// memory.  The chunk's out-rows are contiguous in the forward CSR, so the
+// virtual warp streams the chunk's whole edge range -- coalesced index
+// loads, PUSH_UNROLL per lane in flight -- instead of one row at a time;
+// each lane finds the row of its edge by a cursor over the staged offsets.
 __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
 {
     extern __shared__ uint32_t smem[];
@@ -367,10 +402,23 @@ __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
         for (uint32_t i = lane; i < cnt; i += W) my_c[i] = a.contrib_in[v0 + i];
         for (uint32_t i = lane; i < cnt + 1; i += W) my_off[i] = a.fwd_v[v0 + i];
         __syncwarp(mask);
-        for (uint32_t v = 0; v < cnt; v++) {
-            const float out = my_c[v];
-            for (uint32_t i = my_off[v] + lane; i < my_off[v + 1]; i += W)
-                atomicAdd(&a.acc[__ldg(a.fwd_e + i)], out);
+        const uint32_t e0 = my_off[0], e1 = my_off[cnt];
+        uint32_t r = 0;                              // this lane's row cursor
+        for (uint32_t base = e0; base < e1; base += W * PUSH_UNROLL) {
+            uint32_t d[PUSH_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * W + lane;
+                d[u] = p < e1 ? __ldcs(a.fwd_e + p) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * W + lane;
+                if (p < e1) {
+                    while (my_off[r + 1] <= p) r++;      // ends: my_off[cnt] = e1 > p
+                    atomicAdd(&a.acc[d[u]], my_c[r]);
+                }
+            }
         }
         __syncwarp(mask);
     }
@@ -424,10 +472,15 @@ __device__ __forceinline__ float finish_vertex(const PrArgs &a, uint64_t v, floa
 
 // ----------------------------- pull variants ------------------------------
 // vertex-pull-warp / -nodiv (pagerank/vertex_pull_warp.cu:4-49,
-// vertex_pull_warp_nodiv.cu:4-47): a virtual warp of W lanes per vertex
-// of a C-vertex chunk; lane-strided partial sums are combined with a
-// shuffle tree (the reference adds each lane's partial with a float
-// atomic) and the vertex is consolidated in place.
+// vertex_pull_warp_nodiv.cu:4-47): a virtual warp of W lanes per chunk of C
+// vertices, each vertex consolidated in place.  The reference takes the
+// chunk's vertices one after the other and adds each lane's partial with a
+// float atomic, so its summation order is unspecified.  Here the chunk's
+// in-rows, contiguous in the reverse CSR, are streamed as one edge range:
+// coalesced index loads and PUSH_UNROLL independent gathers per lane in
+// flight; each lane adds the terms of its run of one row in a register and
+// flushes the run into the row's shared-memory accumulator; then the lanes
+// consolidate the chunk's vertices together.
 template<bool NODIV>
 __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
 {
@@ -435,26 +488,52 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
     const uint32_t W = a.warp_size, C = a.chunk_size;
     const uint32_t per_block = blockDim.x / W, vw = threadIdx.x / W, lane = threadIdx.x % W;
     const unsigned mask = W >= 32 ? FULL_MASK : (((1u << W) - 1u) << ((threadIdx.x & 31) & ~(W - 1u)));
-    uint32_t *my_off = smem + vw * (C + 1);
+    float *my_acc = reinterpret_cast<float *>(smem) + vw * C;
+    uint32_t *my_off = smem + per_block * C + vw * (C + 1);
     const uint64_t n = a.n, total = uint64_t(gridDim.x) * per_block;
     const float *src = NODIV ? a.pr_in : a.contrib_in;
     const float base_nd = nodiv_base(n);
+    constexpr uint32_t NO_ROW = 0xffffffffu;
     float dsum = 0.0f;
     for (uint64_t chunk = blockIdx.x * uint64_t(per_block) + vw; chunk * C < n; chunk += total) {
         const uint64_t v0 = chunk * C;
         const uint32_t cnt = static_cast<uint32_t>(min(uint64_t(C), n - v0));
         for (uint32_t i = lane; i < cnt + 1; i += W) my_off[i] = a.rev_v[v0 + i];
+        for (uint32_t i = lane; i < cnt; i += W) my_acc[i] = 0.0f;
         __syncwarp(mask);
-        for (uint32_t v = 0; v < cnt; v++) {
-            float part = 0.0f;
-            for (uint32_t i = my_off[v] + lane; i < my_off[v + 1]; i += W)
-                part += __ldg(src + __ldg(a.rev_e + i));
-            for (uint32_t o = W >> 1; o > 0; o >>= 1) part += __shfl_xor_sync(mask, part, o, W);
-            if (lane == 0) {
-                const uint64_t x = v0 + v;
-                dsum += finish_vertex<NODIV>(a, x, part, base_nd);
+        const uint32_t e0 = my_off[0], e1 = my_off[cnt];
+        uint32_t r = 0, run_row = NO_ROW;            // row cursor; row of the open run
+        float run = 0.0f;
+        for (uint32_t base = e0; base < e1; base += W * PUSH_UNROLL) {
+            uint32_t idx[PUSH_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * W + lane;
+                idx[u] = p < e1 ? __ldcs(a.rev_e + p) : 0u;
+            }
+            float val[PUSH_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * W + lane;
+                val[u] = p < e1 ? __ldcg(src + idx[u]) : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * W + lane;
+                if (p < e1) {
+                    while (my_off[r + 1] <= p) r++;      // ends: my_off[cnt] = e1 > p
+                    if (r != run_row) {
+                        if (run_row != NO_ROW) atomicAdd(&my_acc[run_row], run);
+                        run_row = r;
+                        run = 0.0f;
+                    }
+                    run += val[u];
+                }
             }
         }
+        if (run_row != NO_ROW) atomicAdd(&my_acc[run_row], run);
+        __syncwarp(mask);
+        for (uint32_t i = lane; i < cnt; i += W) dsum += finish_vertex<NODIV>(a, v0 + i, my_acc[i], base_nd);
         __syncwarp(mask);
     }
     add_diff(a.diff, dsum);
@@ -1393,9 +1472,9 @@ Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cf
     const uint32_t C = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
     if (cfg && cfg->block_size) g.block = cfg->block_size;
     if (cfg && cfg->grid_size) g.grid = cfg->grid_size;
-    if (variant == PR_VERTEX_PUSH_WARP) g.smem = (g.block / W) * (C * 4 + (C + 1) * 4);
-    if (variant == PR_VERTEX_PULL_WARP || variant == PR_VERTEX_PULL_WARP_NODIV)
-        g.smem = (g.block / W) * ((C + 1) * 4);
+    // C staged values (push: contributions; pull: accumulators) and C + 1 offsets per virtual warp
+    if (variant == PR_VERTEX_PUSH_WARP || variant == PR_VERTEX_PULL_WARP || variant == PR_VERTEX_PULL_WARP_NODIV)
+        g.smem = (g.block / W) * (C * 4 + (C + 1) * 4);
     return g;
 }
 

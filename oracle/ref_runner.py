@@ -211,7 +211,16 @@ class ReferenceKernels:
         return g
 
     # -- BFS ---------------------------------------------------------------
-    def bfs(self, g, variant: str, root: int, warp: int = 32, chunk: int = 32, max_levels: int = 1 << 20):
+    def _event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.torch.cuda.current_stream())
+        return e
+
+    def bfs(self, g, variant: str, root: int, warp: int = 32, chunk: int = 32, max_levels: int = 1 << 20,
+            times: list | None = None):
+        """Depths and per-level visit counts; with `times`, each level's
+        kernel time (CUDA events around the launch, host round trips
+        excluded) is appended in ms."""
         torch = self.torch
         fam = variant
         red = 0
@@ -239,8 +248,12 @@ class ReferenceKernels:
             if warpk:
                 args += [("u64", warp), ("u64", chunk)]
             args += [("u64", g["struct"][(rep, direction)].data_ptr()), ("u64", levels.data_ptr()), ("i32", curr)]
+            e0 = self._event() if times is not None else None
             self.launch(f, grid, block, smem, args)
+            e1 = self._event() if times is not None else None
             self.sync()
+            if times is not None:
+                times.append(e0.elapsed_time(e1))
             self.drv.ok(self.drv.cu.cuMemcpyDtoH_v2(C.byref(out), fptr, 4), "getFrontier")
             counts.append(out.value)
             curr += 1
@@ -249,7 +262,11 @@ class ReferenceKernels:
         return levels.cpu().numpy(), np.array(counts, dtype=np.uint32)
 
     # -- PageRank ----------------------------------------------------------
-    def pagerank(self, g, variant: str, iterations: int, warp: int = 32, chunk: int = 32):
+    def pagerank(self, g, variant: str, iterations: int, warp: int = 32, chunk: int = 32,
+                 times: list | None = None):
+        """Ranks and per-iteration diffs; with `times`, each iteration's
+        kernel + consolidation time (CUDA events, host round trips excluded)
+        is appended in ms."""
         torch = self.torch
         (kname, rep, direction, div, mem, cons, dname, drep, ddir, ddiv) = _PR_VARIANTS[variant]
         module = "ref_pagerank_pull_warp" if "PullWarp" in kname else "ref_pagerank"
@@ -284,11 +301,15 @@ class ReferenceKernels:
             args = [("u64", warp), ("u64", chunk)] if mem else []
             args += [("u64", g["struct"][(rep, direction)].data_ptr()), ("u64", degp),
                      ("u64", pr.data_ptr()), ("u64", newpr.data_ptr())]
+            e0 = self._event() if times is not None else None
             self.launch(kf, gr, b, smem, args)
             cb, cg = geo("vertex")
             self.launch(cf, cg, cb, 0, [("u64", n), ("u64", degp), ("u64", pr.data_ptr()),
                                         ("u64", newpr.data_ptr()), ("bool", iterations > j)])
+            e1 = self._event() if times is not None else None
             self.sync()
+            if times is not None:
+                times.append(e0.elapsed_time(e1))
             out = C.c_float(0.0)
             self.drv.ok(self.drv.cu.cuMemcpyDtoH_v2(C.byref(out), dptr, 4), "getDiff")
             diffs.append(out.value)
