@@ -17,6 +17,7 @@
 
 #include "bw_consolidate.h"
 #include "bw_internal.cuh"
+#include "bw_seqsum_warp.cuh"
 
 namespace bw {
 namespace {
@@ -28,6 +29,9 @@ constexpr uint32_t BATCH_HEAVY = 1024;    // rows above this are expanded by the
 constexpr uint32_t HEAVY_SLOTS = 256;
 constexpr uint32_t NO_UNIT = 0xffffffffu;
 constexpr float DAMPING = 0.85f;
+constexpr uint32_t BATCH_PR_LIGHT = 64;   // PageRank rows above this are summed by a whole warp
+constexpr int BATCH_PR_UNROLL = 8;
+constexpr uint32_t BATCH_PR_L = 8;        // warp sums: windows of 32 x 8 terms
 
 struct BatchArgs {
     const uint32_t *fwd_v, *fwd_e, *rev_v, *rev_e;
@@ -49,12 +53,14 @@ struct BatchArgs {
 __device__ __forceinline__ bool relax_local(int32_t *lv, uint32_t v, int32_t nd)
 { return lv[v] > nd && atomicMin(&lv[v], nd) > nd; }
 
-__global__ void __launch_bounds__(BATCH_THREADS) k_batch(BatchArgs a)
+__global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
 {
     __shared__ uint32_t s_unit, s_qlen[2], s_heavy_n;
     __shared__ uint32_t s_heavy[HEAVY_SLOTS];
     __shared__ uint32_t s_excl[BATCH_WARPS][32], s_start[BATCH_WARPS][32];
     __shared__ double s_base;
+    __shared__ uint32_t s_long_n, s_job;
+    __shared__ float s_stage[BATCH_WARPS][33 * BATCH_PR_L];
     __shared__ unsigned long long s_trav;
     const unsigned tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
     uint32_t *q[2] = {a.queues + static_cast<size_t>(blockIdx.x) * 2 * a.qcap,
@@ -159,34 +165,87 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch(BatchArgs a)
         for (int o = 16; o > 0; o >>= 1) trav += __shfl_xor_sync(FULL_MASK, trav, o);
         if (lane == 0 && trav) atomicAdd(&s_trav, trav);
         // --------------------------- PageRank -----------------------------
+        // Every row is summed in row order from +0 (bit-identical to the
+        // reference's loop).  Rows of at most BATCH_PR_LIGHT terms: one lane
+        // each, BATCH_PR_UNROLL gathers in flight.  Longer rows: one warp
+        // each (warp_sequential_continue_load: coalesced gathers staged in
+        // shared memory, a serial start by one lane, then binade-map scans),
+        // so that a hub's row no longer holds the CTA's iteration.  Warps take
+        // jobs -- the long rows, then chunks of 32 vertices -- from a
+        // shared-memory counter.
         if (a.mode == BW_BATCH_GRAPHS && a.pr_iters) {
             const uint32_t ng = ve - vb;
-            if (tid == 0) s_base = (1.0 - static_cast<double>(DAMPING)) / static_cast<double>(ng);
+            if (tid == 0) {
+                s_base = (1.0 - static_cast<double>(DAMPING)) / static_cast<double>(ng);
+                s_long_n = 0;
+                s_job = 0;
+            }
             __syncthreads();
             const double base = s_base;
             const float init = __fdiv_rn(1.0f, static_cast<float>(ng));
+            uint32_t *long_rows = q[0];                  // the BFS queues are free now
             for (uint32_t v = vb + tid; v < ve; v += BATCH_THREADS) {
                 const uint32_t d = a.fwd_v[v + 1] - a.fwd_v[v];
                 a.ranks[v] = init;
                 cbuf[0][v - vb] = d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f;
+                if (a.rev_v[v + 1] - a.rev_v[v] > BATCH_PR_LIGHT) long_rows[atomicAdd(&s_long_n, 1u)] = v;
             }
             __syncthreads();
+            const uint32_t n_long = s_long_n, jobs = n_long + (ng + 31) / 32;
+            auto finish = [&](uint32_t v, float sum, float *cout) {
+                const float scaled = __fmul_rn(DAMPING, sum);
+                bool ok;
+                const uint32_t rb = bwcons::add_round_bits(static_cast<uint64_t>(__double_as_longlong(base)),
+                                                           __float_as_uint(scaled), ok);
+                const float nr = ok ? __uint_as_float(rb) : __double2float_rn(__dadd_rn(base, static_cast<double>(scaled)));
+                a.ranks[v] = nr;
+                const uint32_t d = a.fwd_v[v + 1] - a.fwd_v[v];
+                cout[v - vb] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
+            };
             for (uint32_t it = 1; it <= a.pr_iters; it++) {
                 const float *cin = cbuf[(it - 1) & 1];
                 float *cout = cbuf[it & 1];
-                for (uint32_t v = vb + tid; v < ve; v += BATCH_THREADS) {
-                    const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
-                    float sum = 0.0f;
-                    for (uint32_t i = s; i < e; i++) sum = __fadd_rn(sum, cin[__ldg(a.rev_e + i) - vb]);
-                    const float scaled = __fmul_rn(DAMPING, sum);
-                    bool ok;
-                    const uint32_t rb = bwcons::add_round_bits(static_cast<uint64_t>(__double_as_longlong(base)),
-                                                               __float_as_uint(scaled), ok);
-                    const float nr = ok ? __uint_as_float(rb) : __double2float_rn(__dadd_rn(base, static_cast<double>(scaled)));
-                    a.ranks[v] = nr;
-                    const uint32_t d = a.fwd_v[v + 1] - a.fwd_v[v];
-                    cout[v - vb] = d ? __fdiv_rn(nr, static_cast<float>(d)) : 0.0f;
+                for (;;) {
+                    uint32_t job = 0;
+                    if (lane == 0) job = atomicAdd(&s_job, 1u);
+                    job = __shfl_sync(FULL_MASK, job, 0);
+                    if (job >= jobs) break;
+                    if (job < n_long) {
+                        const uint32_t v = long_rows[job];
+                        const uint32_t s = a.rev_v[v], len = a.rev_v[v + 1] - s;
+                        auto load = [&](uint32_t i) { return cin[__ldg(a.rev_e + s + i) - vb]; };
+                        uint32_t sb = 0;
+                        float sum;
+                        if (warp_sequential_continue_load<BATCH_PR_L>(load, 0, len, sb, s_stage[wib], lane)) {
+                            sum = __uint_as_float(sb);
+                        } else {                         // terms outside the maps' domain: the plain loop
+                            sum = 0.0f;
+                            if (lane == 0)
+                                for (uint32_t i = 0; i < len; i++) sum = __fadd_rn(sum, load(i));
+                        }
+                        if (lane == 0) finish(v, sum, cout);
+                    } else {
+                        const uint32_t v = vb + (job - n_long) * 32 + lane;
+                        if (v < ve) {
+                            const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
+                            if (e - s <= BATCH_PR_LIGHT) {
+                                float sum = 0.0f;
+                                for (uint32_t i = s; i < e; i += BATCH_PR_UNROLL) {
+                                    float t[BATCH_PR_UNROLL];
+#pragma unroll
+                                    for (int k = 0; k < BATCH_PR_UNROLL; k++)
+                                        t[k] = i + k < e ? cin[__ldg(a.rev_e + i + k) - vb] : 0.0f;
+#pragma unroll
+                                    for (int k = 0; k < BATCH_PR_UNROLL; k++)
+                                        if (i + k < e) sum = __fadd_rn(sum, t[k]);
+                                }
+                                finish(v, sum, cout);
+                            }
+                        }
+                    }
                 }
+                __syncthreads();
+                if (tid == 0) s_job = 0;
                 __syncthreads();
             }
         }
