@@ -11,6 +11,7 @@
 // reference's consolidation (pagerank/vertex_pull.cu:23-29,
 // pagerank/pagerank.cu:131-136), so ranks are bit-identical to a
 // single-graph vertex-pull run.
+#include <algorithm>
 #include <climits>
 
 #include <cooperative_groups.h>
@@ -31,6 +32,7 @@ constexpr uint32_t NO_UNIT = 0xffffffffu;
 constexpr float DAMPING = 0.85f;
 constexpr uint32_t BATCH_PR_LIGHT = 64;   // PageRank rows above this are summed by a whole warp
 constexpr int BATCH_PR_UNROLL = 8;
+constexpr int BATCH_BFS_UNROLL = 4;
 constexpr uint32_t BATCH_PR_L = 8;        // warp sums: windows of 32 x 8 terms
 
 struct BatchArgs {
@@ -47,6 +49,7 @@ struct BatchArgs {
     int32_t *levels;
     float *ranks;
     uint32_t pr_iters;
+    uint32_t vis_words;       // > 0: the unit's visited set is a shared-memory bitmap of this many words
     unsigned long long *traversed;
 };
 
@@ -61,6 +64,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
     __shared__ double s_base;
     __shared__ uint32_t s_long_n, s_job;
     __shared__ float s_stage[BATCH_WARPS][33 * BATCH_PR_L];
+    extern __shared__ uint32_t s_vis[];
     __shared__ unsigned long long s_trav;
     const unsigned tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
     uint32_t *q[2] = {a.queues + static_cast<size_t>(blockIdx.x) * 2 * a.qcap,
@@ -89,7 +93,13 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
         }
         const uint32_t root = a.roots[unit];
         for (uint32_t v = vb + tid; v < ve; v += BATCH_THREADS) lv[v] = v == root ? 0 : INF;
+        const bool bitmap = a.vis_words != 0;
+        if (bitmap) {
+            for (uint32_t w = tid; w < (ve - vb + 31) / 32; w += BATCH_THREADS) s_vis[w] = 0u;
+            __syncthreads();
+        }
         if (tid == 0) {
+            if (bitmap) s_vis[(root - vb) >> 5] = 1u << ((root - vb) & 31);
             q[0][0] = root;
             s_qlen[0] = 1;
             s_qlen[1] = 0;
@@ -104,8 +114,19 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
             const uint32_t *qin = q[depth & 1];
             uint32_t *qout = q[(depth + 1) & 1];
             uint32_t *olen = &s_qlen[(depth + 1) & 1];
+            // first visit of u: the shared-memory bitmap answers without a
+            // global access (and its atomic is a shared one); the depth is
+            // then stored once
+            auto relax = [&](uint32_t u) -> bool {
+                if (!bitmap) return relax_local(lv, u, nd);
+                const uint32_t w = (u - vb) >> 5, bit = 1u << ((u - vb) & 31);
+                if (s_vis[w] & bit) return false;
+                if (atomicOr(&s_vis[w], bit) & bit) return false;
+                lv[u] = nd;
+                return true;
+            };
             auto visit = [&](uint32_t u) {
-                if (relax_local(lv, u, nd)) {
+                if (relax(u)) {
                     cg::coalesced_group g = cg::coalesced_threads();
                     uint32_t base = 0;
                     if (g.thread_rank() == 0) base = atomicAdd(olen, g.size());
@@ -134,13 +155,24 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
                 s_excl[wib][lane] = incl - d;
                 s_start[wib][lane] = s;
                 __syncwarp();
-                for (uint32_t k = lane; k < total; k += 32) {
-                    int lo = 0, hi = 31;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
+                // edge k of the 32 concatenated rows: a per-lane cursor over
+                // the rows' exclusive offsets (k grows), BATCH_BFS_UNROLL
+                // neighbours' indices in flight before their visits
+                uint32_t seg = 0;
+                for (uint32_t k0 = 0; k0 < total; k0 += 32 * BATCH_BFS_UNROLL) {
+                    uint32_t u[BATCH_BFS_UNROLL];
+#pragma unroll
+                    for (int j = 0; j < BATCH_BFS_UNROLL; j++) {
+                        const uint32_t k = k0 + j * 32 + lane;
+                        u[j] = NO_UNIT;
+                        if (k < total) {
+                            while (seg < 31 && s_excl[wib][seg + 1] <= k) seg++;
+                            u[j] = __ldg(a.fwd_e + s_start[wib][seg] + (k - s_excl[wib][seg]));
+                        }
                     }
-                    visit(__ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo])));
+#pragma unroll
+                    for (int j = 0; j < BATCH_BFS_UNROLL; j++)
+                        if (u[j] != NO_UNIT) visit(u[j]);
                 }
                 __syncwarp();
             }
@@ -149,7 +181,17 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
             for (uint32_t h = 0; h < heavy; h++) {
                 const uint32_t v = s_heavy[h];
                 const uint32_t s = a.fwd_v[v], e = a.fwd_v[v + 1];
-                for (uint32_t i = s + tid; i < e; i += BATCH_THREADS) visit(__ldg(a.fwd_e + i));
+                for (uint32_t i0 = s; i0 < e; i0 += BATCH_THREADS * BATCH_BFS_UNROLL) {
+                    uint32_t u[BATCH_BFS_UNROLL];
+#pragma unroll
+                    for (int j = 0; j < BATCH_BFS_UNROLL; j++) {
+                        const uint32_t i = i0 + j * BATCH_THREADS + tid;
+                        u[j] = i < e ? __ldg(a.fwd_e + i) : NO_UNIT;
+                    }
+#pragma unroll
+                    for (int j = 0; j < BATCH_BFS_UNROLL; j++)
+                        if (u[j] != NO_UNIT) visit(u[j]);
+                }
             }
             __syncthreads();
             if (tid == 0) {
@@ -278,7 +320,17 @@ extern "C" int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode, c
         return BW_OK;
     }
     cudaStream_t s = as_stream(stream);
-    unsigned grid = static_cast<unsigned>(ctx->sm_count) * 2;
+    // the visited bitmap of the largest unit in shared memory when it fits
+    // beside the kernel's static shared memory; CTAs per SM as it allows
+    cudaFuncAttributes fa{};
+    BW_CUDA(cudaFuncGetAttributes(&fa, k_batch));
+    const uint64_t words = (static_cast<uint64_t>(max_unit_vertices) + 31) / 32;
+    const bool bitmap = fa.sharedSizeBytes + words * 4 + 1024 <= static_cast<uint64_t>(ctx->max_smem_optin);
+    const size_t dyn = bitmap ? words * 4 : 0;
+    BW_CUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    int per_sm = 0;
+    BW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, BATCH_THREADS, dyn));
+    unsigned grid = static_cast<unsigned>(ctx->sm_count) * static_cast<unsigned>(std::max(1, std::min(per_sm, 2)));
     if (cfg && cfg->grid_size) grid = cfg->grid_size;
     if (cfg && cfg->block_size && cfg->block_size != BATCH_THREADS) return BW_ERR_INVALID_ARGUMENT;
     BatchArgs a{};
@@ -293,6 +345,7 @@ extern "C" int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode, c
     a.levels = levels;
     a.ranks = ranks;
     a.pr_iters = mode == BW_BATCH_GRAPHS ? pr_iterations : 0;
+    a.vis_words = bitmap ? static_cast<uint32_t>(words) : 0u;
     const size_t per_cta = static_cast<size_t>(2) * max_unit_vertices;
     char *scratch = nullptr;
     const size_t bytes = 64 + grid * per_cta * sizeof(uint32_t) + (a.pr_iters ? grid * per_cta * sizeof(float) : 0);
@@ -303,7 +356,7 @@ extern "C" int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode, c
     a.queues = reinterpret_cast<uint32_t *>(scratch + 64);
     a.contrib = a.pr_iters ? reinterpret_cast<float *>(scratch + 64 + grid * per_cta * sizeof(uint32_t)) : nullptr;
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
-    k_batch<<<grid, BATCH_THREADS, 0, s>>>(a);
+    k_batch<<<grid, BATCH_THREADS, dyn, s>>>(a);
     BW_CUDA(cudaGetLastError());
     BW_CUDA(cudaEventRecord(ctx->ev_stop, s));
     unsigned long long trav = 0;
