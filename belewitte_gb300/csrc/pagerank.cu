@@ -92,6 +92,13 @@ struct PrArgs {
     float *piece_sum;             // exact pieces: float sum of the piece's terms (any order)
     uint4 *piece_map;             // giant-row pieces: two-uint4 records (k_pr_long_sums)
     uint32_t *sum_ctr;            // k_pr_long_sums' job and finish counters
+    // Heavy units of the push and warp-pull variants (rows or chunks with
+    // too many edges for one warp), cut into tiles that every warp of a
+    // second kernel shares:
+    uint4 *heavy_q;               // {unit, first edge, end edge, 0}
+    uint32_t *heavy_ctr;          // [0] tiles queued, [1] taken, [2] warps done, [3] chunks listed, [4] warps done
+    uint32_t *heavy_chunks;       // warp-pull: heavy chunks, consolidated by k_pr_heavy_finish
+    uint32_t heavy_cap;           // capacity of heavy_q
     // Decided on the device, so the host never waits inside a run:
     const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
@@ -347,6 +354,27 @@ __global__ void __launch_bounds__(256) k_pr_edge(PrArgs a)
 constexpr uint32_t PUSH_HEAVY = 32;
 constexpr int PUSH_UNROLL = 8;
 
+// A row (vertex-push) or a chunk (the virtual-warp variants) with more than
+// HEAVY_UNIT edges would hold one warp for the whole iteration on a skewed
+// graph -- R-MAT's hubs share the lowest ids.  Its edge range is queued
+// instead, in HEAVY_TILE-edge tiles that every warp of k_pr_heavy_tiles
+// takes from a counter.  The queue holds at most M / HEAVY_TILE +
+// M / (the unit threshold) + 1 tiles.
+constexpr uint32_t HEAVY_UNIT = 8192;
+constexpr uint32_t HEAVY_TILE = 2048;
+// vertex-push: a warp expands its rows of more than PUSH_HEAVY edges one
+// after the other, so rows above PUSH_GIANT go to the tiles already
+constexpr uint32_t PUSH_GIANT = 1024;
+
+__device__ __forceinline__ void enqueue_tiles(const PrArgs &a, uint32_t unit, uint32_t t0, uint32_t t1)
+{
+    const uint32_t cnt = (t1 - t0 + HEAVY_TILE - 1) / HEAVY_TILE;
+    const uint32_t base = atomicAdd(&a.heavy_ctr[0], cnt);
+    for (uint32_t k = 0; k < cnt; k++)
+        if (base + k < a.heavy_cap)
+            a.heavy_q[base + k] = make_uint4(unit, t0 + k * HEAVY_TILE, min(t1, t0 + (k + 1) * HEAVY_TILE), 0u);
+}
+
 __global__ void __launch_bounds__(256) k_pr_vertex_push(PrArgs a)
 {
     const unsigned lane = threadIdx.x & 31;
@@ -358,8 +386,10 @@ __global__ void __launch_bounds__(256) k_pr_vertex_push(PrArgs a)
             e = a.fwd_v[v + 1];
         }
         const float out = s < e ? a.contrib_in[v] : 0.0f;
-        const bool heavy = e - s > PUSH_HEAVY;
-        if (!heavy) {
+        const bool giant = e - s > PUSH_GIANT;
+        if (giant) enqueue_tiles(a, static_cast<uint32_t>(v), s, e);
+        const bool heavy = !giant && e - s > PUSH_HEAVY;
+        if (!heavy && !giant) {
 #pragma unroll 4
             for (uint32_t i = s; i < e; i++) atomicAdd(&a.acc[__ldg(a.fwd_e + i)], out);
         }
@@ -404,8 +434,10 @@ __global__ void __launch_bounds__(512) k_pr_vertex_push_warp(PrArgs a)
         for (uint32_t i = lane; i < cnt + 1; i += W) my_off[i] = a.fwd_v[v0 + i];
         __syncwarp(mask);
         const uint32_t e0 = my_off[0], e1 = my_off[cnt];
+        const bool heavy = e1 - e0 > HEAVY_UNIT;       // tiles for k_pr_heavy_tiles
+        if (heavy && lane == 0) enqueue_tiles(a, static_cast<uint32_t>(chunk), e0, e1);
         uint32_t r = 0;                              // this lane's row cursor
-        for (uint32_t base = e0; base < e1; base += W * PUSH_UNROLL) {
+        for (uint32_t base = e0; base < (heavy ? e0 : e1); base += W * PUSH_UNROLL) {
             uint32_t d[PUSH_UNROLL];
 #pragma unroll
             for (int u = 0; u < PUSH_UNROLL; u++) {
@@ -503,6 +535,14 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
         for (uint32_t i = lane; i < cnt; i += W) my_acc[i] = 0.0f;
         __syncwarp(mask);
         const uint32_t e0 = my_off[0], e1 = my_off[cnt];
+        if (e1 - e0 > HEAVY_UNIT) {                  // summed by k_pr_heavy_tiles, finished by k_pr_heavy_finish
+            if (lane == 0) {
+                enqueue_tiles(a, static_cast<uint32_t>(chunk), e0, e1);
+                a.heavy_chunks[atomicAdd(&a.heavy_ctr[3], 1u)] = static_cast<uint32_t>(chunk);
+            }
+            __syncwarp(mask);
+            continue;
+        }
         uint32_t r = 0, run_row = NO_ROW;            // row cursor; row of the open run
         float run = 0.0f;
         for (uint32_t base = e0; base < e1; base += W * PUSH_UNROLL) {
@@ -538,6 +578,128 @@ __global__ void __launch_bounds__(512) k_pr_vertex_pull_warp(PrArgs a)
         __syncwarp(mask);
     }
     add_diff(a.diff, dsum);
+}
+
+// Tiles of the heavy units queued by this iteration's first kernel
+// (enqueue_tiles), taken by every warp from a counter; the last warp out
+// resets the counters.  The push modes add each edge's contribution to its
+// destination with a float atomic, as the first kernel does.  The pull
+// modes add each lane's run of one row into acc[row] with a float atomic
+// (the reference's warp kernels add lane partials with atomics too), and
+// k_pr_heavy_finish consolidates the rows.
+template<int MODE>   // 0 vertex-push, 1 vertex-push-warp, 2 vertex-pull-warp, 3 vertex-pull-warp-nodiv
+__global__ void __launch_bounds__(256) k_pr_heavy_tiles(PrArgs a)
+{
+    constexpr uint32_t NO_ROW = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31;
+    const uint32_t tiles = min(a.heavy_ctr[0], a.heavy_cap);
+    const uint32_t *V = MODE <= 1 ? a.fwd_v : a.rev_v;
+    const uint32_t *E = MODE <= 1 ? a.fwd_e : a.rev_e;
+    const float *src = MODE == 3 ? a.pr_in : a.contrib_in;
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&a.heavy_ctr[1], 1u);
+        t = __shfl_sync(FULL_MASK, t, 0);
+        if (t >= tiles) break;
+        const uint4 q = a.heavy_q[t];
+        const uint32_t t0 = q.y, t1 = q.z;
+        if constexpr (MODE == 0) {                   // one row: its contribution to every edge
+            const float c = a.contrib_in[q.x];
+            for (uint32_t base = t0; base < t1; base += 32 * PUSH_UNROLL) {
+                uint32_t d[PUSH_UNROLL];
+#pragma unroll
+                for (int u = 0; u < PUSH_UNROLL; u++) {
+                    const uint32_t i = base + u * 32 + lane;
+                    d[u] = i < t1 ? __ldcs(E + i) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < PUSH_UNROLL; u++)
+                    if (base + u * 32 + lane < t1) atomicAdd(&a.acc[d[u]], c);
+            }
+            continue;
+        }
+        // a chunk's rows v0 .. v0 + cnt - 1: the row of edge t0 by bisection,
+        // then a cursor per lane
+        const uint64_t v0 = uint64_t(q.x) * a.chunk_size;
+        const uint32_t cnt = static_cast<uint32_t>(min(uint64_t(a.chunk_size), a.n - v0));
+        uint32_t lo = 0, hi = cnt - 1;                // the last r with V[v0 + r] <= t0
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (V[v0 + mid] <= t0) lo = mid; else hi = mid - 1;
+        }
+        uint32_t r = lo, run_row = NO_ROW;
+        float run = 0.0f;
+        for (uint32_t base = t0; base < t1; base += 32 * PUSH_UNROLL) {
+            uint32_t idx[PUSH_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * 32 + lane;
+                idx[u] = p < t1 ? __ldcs(E + p) : 0u;
+            }
+            float val[PUSH_UNROLL];
+            if constexpr (MODE >= 2) {
+#pragma unroll
+                for (int u = 0; u < PUSH_UNROLL; u++) {
+                    const uint32_t p = base + u * 32 + lane;
+                    val[u] = p < t1 ? __ldcg(src + idx[u]) : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; u++) {
+                const uint32_t p = base + u * 32 + lane;
+                if (p < t1) {
+                    while (V[v0 + r + 1] <= p) r++;      // ends: V[v0 + cnt] >= t1 > p
+                    if constexpr (MODE == 1) {
+                        atomicAdd(&a.acc[idx[u]], a.contrib_in[v0 + r]);
+                    } else {
+                        if (r != run_row) {
+                            if (run_row != NO_ROW) atomicAdd(&a.acc[v0 + run_row], run);
+                            run_row = r;
+                            run = 0.0f;
+                        }
+                        run += val[u];
+                    }
+                }
+            }
+        }
+        if constexpr (MODE >= 2)
+            if (run_row != NO_ROW) atomicAdd(&a.acc[v0 + run_row], run);
+    }
+    if (lane == 0) {
+        const uint32_t warps = gridDim.x * (blockDim.x / 32);
+        if (atomicAdd(&a.heavy_ctr[2], 1u) + 1 == warps) {
+            a.heavy_ctr[0] = 0;
+            a.heavy_ctr[1] = 0;
+            a.heavy_ctr[2] = 0;
+        }
+    }
+}
+
+// Consolidates the rows of the heavy chunks of the warp-pull variants from
+// acc[] (summed by k_pr_heavy_tiles) and clears acc[] for the next
+// iteration; the last warp out resets the chunk list.
+template<bool NODIV>
+__global__ void __launch_bounds__(256) k_pr_heavy_finish(PrArgs a)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    const uint32_t chunks = a.heavy_ctr[3];
+    const float base_nd = nodiv_base(a.n);
+    float dsum = 0.0f;
+    for (uint64_t k = warp; k < chunks; k += warps) {
+        const uint64_t v0 = uint64_t(a.heavy_chunks[k]) * a.chunk_size;
+        const uint32_t cnt = static_cast<uint32_t>(min(uint64_t(a.chunk_size), a.n - v0));
+        for (uint32_t i = lane; i < cnt; i += 32) {
+            const float sum = a.acc[v0 + i];
+            a.acc[v0 + i] = 0.0f;
+            dsum += finish_vertex<NODIV>(a, v0 + i, sum, base_nd);
+        }
+    }
+    add_diff(a.diff, dsum);
+    if (lane == 0 && atomicAdd(&a.heavy_ctr[4], 1u) + 1 == warps) {
+        a.heavy_ctr[3] = 0;
+        a.heavy_ctr[4] = 0;
+    }
 }
 
 // ------------------------- work-list pull kernels ---------------------------
@@ -1520,8 +1682,16 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_REV_EDGE_LIST: k_pr_edge<1><<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_STRUCT_EDGE_LIST: k_pr_edge<2><<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_REV_STRUCT_EDGE_LIST: k_pr_edge<3><<<geo.grid, geo.block, 0, s>>>(a); break;
-      case PR_VERTEX_PUSH: k_pr_vertex_push<<<geo.grid, geo.block, 0, s>>>(a); break;
-      case PR_VERTEX_PUSH_WARP: k_pr_vertex_push_warp<<<geo.grid, geo.block, geo.smem, s>>>(a); break;
+      case PR_VERTEX_PUSH:
+        k_pr_vertex_push<<<geo.grid, geo.block, 0, s>>>(a);
+        k_pr_heavy_tiles<0><<<ctx->sm_count * 4, 256, 0, s>>>(a);
+        ctx->launches++;
+        break;
+      case PR_VERTEX_PUSH_WARP:
+        k_pr_vertex_push_warp<<<geo.grid, geo.block, geo.smem, s>>>(a);
+        k_pr_heavy_tiles<1><<<ctx->sm_count * 4, 256, 0, s>>>(a);
+        ctx->launches++;
+        break;
       case PR_VERTEX_PULL:
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
@@ -1534,8 +1704,18 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         k_pr_long_sums<true><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
-      case PR_VERTEX_PULL_WARP: k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
-      case PR_VERTEX_PULL_WARP_NODIV: k_pr_vertex_pull_warp<true><<<geo.grid, geo.block, geo.smem, s>>>(a); break;
+      case PR_VERTEX_PULL_WARP:
+        k_pr_vertex_pull_warp<false><<<geo.grid, geo.block, geo.smem, s>>>(a);
+        k_pr_heavy_tiles<2><<<ctx->sm_count * 4, 256, 0, s>>>(a);
+        k_pr_heavy_finish<false><<<ctx->sm_count * 2, 256, 0, s>>>(a);
+        ctx->launches += 2;
+        break;
+      case PR_VERTEX_PULL_WARP_NODIV:
+        k_pr_vertex_pull_warp<true><<<geo.grid, geo.block, geo.smem, s>>>(a);
+        k_pr_heavy_tiles<3><<<ctx->sm_count * 4, 256, 0, s>>>(a);
+        k_pr_heavy_finish<true><<<ctx->sm_count * 2, 256, 0, s>>>(a);
+        ctx->launches += 2;
+        break;
       case PR_PULL_SEGMENTED:
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
@@ -1617,7 +1797,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         return BW_ERR_INVALID_ARGUMENT;
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
-    bool need_split = false, need_exact = false, any_rowlen = false, any_deg = false, all_items = true;
+    bool need_split = false, need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
+         all_items = true;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
         all_items = all_items && (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV || v == PR_PULL_SEGMENTED);
@@ -1627,6 +1808,9 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         reps |= kPrReps[v];
         if (v == PR_PULL_SEGMENTED) need_split = true;
         if (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV) need_exact = true;
+        if (v == PR_VERTEX_PUSH || v == PR_VERTEX_PUSH_WARP || v == PR_VERTEX_PULL_WARP ||
+            v == PR_VERTEX_PULL_WARP_NODIV)
+            need_heavy = true;
         if (uses_rowlen(v)) any_rowlen = true; else any_deg = true;
     }
     BW_TRY(check_reps(g, reps));
@@ -1640,6 +1824,17 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     PrRun split_run, exact_run;
     if (need_split) BW_TRY(build_segments(ctx, g, 1, split_run, s));
     if (need_exact) BW_TRY(build_segments(ctx, g, 0, exact_run, s));
+    // heavy-unit tiles of the push and warp-pull variants
+    uint4 *heavy_q = nullptr;
+    uint32_t *heavy_small = nullptr;                 // 8 counters, then the chunk list
+    const uint32_t chunk_c = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
+    const uint64_t heavy_cap = g->edge_count / HEAVY_TILE + g->edge_count / PUSH_GIANT + 2;
+    if (need_heavy) {
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&heavy_q), heavy_cap * sizeof(uint4), s));
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&heavy_small),
+                                 (8 + n / chunk_c + 1) * sizeof(uint32_t), s));
+        BW_CUDA(cudaMemsetAsync(heavy_small, 0, 8 * sizeof(uint32_t), s));
+    }
 
     PrArgs a{};
     a.fwd_v = g->fwd_vertices; a.fwd_e = g->fwd_edges; a.rev_v = g->rev_vertices; a.rev_e = g->rev_edges;
@@ -1676,6 +1871,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     }
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
     a.chunk_size = (cfg && cfg->chunk_size) ? cfg->chunk_size : 32;
+    a.heavy_q = heavy_q;
+    a.heavy_ctr = heavy_small;
+    a.heavy_chunks = heavy_small ? heavy_small + 8 : nullptr;
+    a.heavy_cap = static_cast<uint32_t>(heavy_cap);
 
     BW_CUDA(cudaEventRecord(ctx->ev_start, s));
     // Degrees inside the timed region, as pagerank/pagerank.cpp:102-112.
@@ -1777,6 +1976,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     free_run(split_run, s);
     free_run(exact_run, s);
     free_relabel(rl, s);
+    if (heavy_q) cudaFreeAsync(heavy_q, s);
+    if (heavy_small) cudaFreeAsync(heavy_small, s);
     if (time_iterations && iteration_ms) {
         for (uint32_t j = 0; j < iterations; j++)
             BW_CUDA(cudaEventElapsedTime(&iteration_ms[j], ctx->level_events[j], ctx->level_events[j + 1]));
