@@ -25,6 +25,7 @@ The same JSON line carries:
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --case pagerank:VARIANT:rmat22|er[:BLOCK:HUBS]   (small profiling case)
   python bench.py --case bfs:VARIANT:rmat22            (small profiling case)
+  python bench.py --sweep      (every PageRank variant on R-MAT-22 and ER, us per iteration)
 
 N > 1 (torch.distributed.run): the path does not shard one graph, so each
 rank runs an independent replica (weak scaling).  --impl reference times the
@@ -494,6 +495,28 @@ def run_case(spec: str):
     print("case done", spec)
 
 
+def sweep():
+    """Every PageRank variant, 30 iterations, on R-MAT scale 22 and ER(4M, 67M):
+    the per-iteration median (CUDA events per iteration) as one JSON line
+    per graph."""
+    import torch
+
+    import belewitte_gb300 as bw
+    ctx = bw.Context(0)
+    for label, kind, kw in (("R-MAT scale 22 edge factor 16 seed 22", "rmat", dict(scale=22, edge_factor=16, seed=22)),
+                            ("ER n=4194304 m=67108864 seed 23", "er", dict(n=4194304, m=67108864, seed=23))):
+        g = bw.DeviceGraph.generate(kind, reps=63, **kw)
+        out = {}
+        for v in bw.pagerank_variant_names():
+            bw.pagerank(ctx, g, v, 3)
+            run = bw.pagerank_schedule(ctx, g, [v], ITERATIONS, time_iterations=True)
+            out[v] = round(float(np.median(run.iteration_ms)) * 1e3, 1)
+        print(json.dumps({"graph": label, "vertices": g.vertex_count, "edges": g.edge_count,
+                          "us_per_iteration": out}), flush=True)
+        del g
+        torch.cuda.empty_cache()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -506,7 +529,11 @@ def main():
     ap.add_argument("--no-bfs", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--case", default="")
+    ap.add_argument("--sweep", action="store_true")
     args = ap.parse_args()
+    if args.sweep:
+        sweep()
+        return
     if args.case:
         run_case(args.case)
         return
