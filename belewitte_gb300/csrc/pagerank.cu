@@ -1922,9 +1922,24 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     ctx->launches++;
     BW_CUDA(cudaGetLastError());
 
-    for (uint32_t j = 1; j <= iterations; j++) {
+    // loop_mode 1: the iterations are captured (on a private stream: the
+    // caller's may be the legacy default stream, which cannot capture) into
+    // one CUDA graph that is then launched once on the caller's stream; the
+    // launches and their order are the same
+    cudaGraph_t loop_graph = nullptr;
+    cudaStream_t ls = s;
+    if (loop_mode == 1) {
+        BW_CUDA(cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking));
+        const cudaError_t e = cudaStreamBeginCapture(ls, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(ls);
+            BW_CUDA(e);
+        }
+    }
+    int loop_status = BW_OK;
+    for (uint32_t j = 1; j <= iterations && loop_status == BW_OK; j++) {
         const int v = schedule[std::min<uint32_t>(j - 1, schedule_len - 1)];
-        if (time_iterations) BW_CUDA(cudaEventRecord(ctx->level_events[j - 1], s));
+        if (time_iterations) BW_CUDA(cudaEventRecord(ctx->level_events[j - 1], ls));
         a.not_last = iterations > j ? 1 : 0;
         a.diff = ctx->pr_diffs + (j - 1);
         if (nodiv) {
@@ -1961,9 +1976,28 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         // both buffers once iterations 1 and 2 have written them
         a.count_dev = items.work ? ((!nodiv && j > 2) ? items.count_nonconst : items.count_all) : nullptr;
         Geometry geo = geometry(ctx, v, cfg);
-        BW_TRY(launch_iteration(ctx, v, a, geo, s));
-        (void) loop_mode;
+        loop_status = launch_iteration(ctx, v, a, geo, ls);
     }
+    if (loop_mode == 1) {
+        const cudaError_t e = cudaStreamEndCapture(ls, &loop_graph);
+        cudaStreamDestroy(ls);
+        if (loop_status == BW_OK && e != cudaSuccess) {
+            set_last_error(e, "cudaStreamEndCapture");
+            loop_status = BW_ERR_CUDA;
+        }
+        if (loop_status == BW_OK) {
+            cudaGraphExec_t exec = nullptr;
+            cudaError_t le = cudaGraphInstantiate(&exec, loop_graph, 0);
+            if (le == cudaSuccess) le = cudaGraphLaunch(exec, s);
+            if (exec) cudaGraphExecDestroy(exec);
+            if (le != cudaSuccess) {
+                set_last_error(le, "PageRank iteration graph");
+                loop_status = BW_ERR_CUDA;
+            }
+        }
+        if (loop_graph) cudaGraphDestroy(loop_graph);
+    }
+    BW_TRY(loop_status);
     if (time_iterations) BW_CUDA(cudaEventRecord(ctx->level_events[iterations], s));
     BW_CUDA(cudaEventRecord(ctx->ev_stop, s));
     float diffs_dev_last = 0.0f;

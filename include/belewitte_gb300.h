@@ -360,6 +360,9 @@ typedef struct bw_pagerank_result {
  * inside the call, as the reference does inside its timed region
  * (pagerank/pagerank.cpp:102-112).  `diffs` (optional, host) receives the
  * per-iteration diff the reference reads back (pagerank.cpp:124).
+ * loop_mode 0 launches the iterations from the host; 1 captures them into
+ * one CUDA graph and launches it once (the same kernels in the same order;
+ * the call must not itself be made inside a stream capture).
  */
 int bw_pagerank_run(bw_context *ctx, const bw_graph_view *g, int variant,
                     uint32_t iterations, float *ranks,

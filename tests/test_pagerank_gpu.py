@@ -217,3 +217,18 @@ def test_gather_probe(ctx):
     want = float(src[idx[ok].long()].double().sum().item())
     assert bw.gather_probe_sum(ctx, src, idx) == want         # small integers: exact in any order
     assert bw.gather_ceiling(ctx, src, idx, warmup=1, repeats=3) > 1e9
+
+
+@pytest.mark.parametrize("variant", ["vertex-pull", "pull-segmented", "vertex-push", "vertex-pull-warp-nodiv",
+                                     "rev-edge-list"])
+def test_graph_loop_matches_host_loop(ctx, graphs, long_graphs, variant):
+    """loop="graph" (the iterations captured into one CUDA graph) gives the
+    host loop's ranks: bit for bit where the variant is deterministic,
+    within the reference tolerance where it adds with float atomics."""
+    for name, (h, g) in [("rmat14", graphs["rmat14"]), ("star", graphs["star"])] + list(long_graphs.items()):
+        want = bw.pagerank(ctx, g, variant, 12).ranks.cpu().numpy()
+        got = bw.pagerank(ctx, g, variant, 12, loop="graph").ranks.cpu().numpy()
+        if variant in BITEXACT:
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (variant, name)
+        else:
+            assert _rel(got, want) <= REL_REF, (variant, name)
