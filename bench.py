@@ -25,7 +25,8 @@ The same JSON line carries:
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --case pagerank:VARIANT:rmat22|er[:BLOCK:HUBS]   (small profiling case)
   python bench.py --case bfs:VARIANT:rmat22            (small profiling case)
-  python bench.py --sweep      (every PageRank variant on R-MAT-22 and ER, us per iteration)
+  python bench.py --sweep      (every PageRank variant on R-MAT-22 and ER, every BFS variant
+                                on R-MAT-24 sym, the grid and BA)
 
 N > 1 (torch.distributed.run): the path does not shard one graph, so each
 rank runs an independent replica (weak scaling).  --impl reference times the
@@ -498,7 +499,9 @@ def run_case(spec: str):
 def sweep():
     """Every PageRank variant, 30 iterations, on R-MAT scale 22 and ER(4M, 67M):
     the per-iteration median (CUDA events per iteration) as one JSON line
-    per graph."""
+    per graph; then every BFS variant and the learned switch on the
+    symmetrised R-MAT-24, the 4096 x 4096 grid and BA(8M, 8), one
+    traversal each from the highest-degree vertex."""
     import torch
 
     import belewitte_gb300 as bw
@@ -514,6 +517,36 @@ def sweep():
         print(json.dumps({"graph": label, "vertices": g.vertex_count, "edges": g.edge_count,
                           "us_per_iteration": out}), flush=True)
         del g
+        torch.cuda.empty_cache()
+    # BFS: every variant from the highest-degree vertex (device loop), and
+    # the learned switch; depths checked identical to frontier-push
+    from belewitte_gb300 import learn
+    pred = learn.load_predictor()
+    for label, kind, kw in (("R-MAT scale 24 symmetrised seed 24", "rmat",
+                             dict(scale=24, edge_factor=16, seed=24, symmetrise=True)),
+                            ("grid 4096 x 4096", "grid", dict(h=4096, w=4096)),
+                            ("BA n=8388608 m=8 seed 8", "ba", dict(n=8388608, m=8, seed=8))):
+        g = bw.DeviceGraph.generate(kind, reps=63, **kw)
+        root = int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item())
+        want = bw.bfs(ctx, g, "frontier-push", root, loop="graph")
+        ms, skipped = {}, []
+        for v in bw.bfs_variant_names() + ["learned"]:
+            if kind == "grid" and not v.startswith("frontier") and v != "learned":
+                skipped.append(v)                   # O(N) or O(M) work per level x 8190 levels
+                continue
+            if v == "learned":
+                learn.run_learned(ctx, g, pred, root, loop="graph", stats=False)
+                run = learn.run_learned(ctx, g, pred, root, loop="graph", stats=False)
+            else:
+                bw.bfs(ctx, g, v, root, loop="graph")
+                run = bw.bfs(ctx, g, v, root, loop="graph")
+            if not torch.equal(run.levels, want.levels):
+                raise AssertionError(f"BFS depths of {v} differ")
+            ms[v] = round(run.device_ms, 3)
+        print(json.dumps({"graph": label, "vertices": g.vertex_count, "edges": g.edge_count, "root": root,
+                          "levels": want.level_count, "traversed_edges": want.traversed_edges,
+                          "ms_per_bfs": ms, "not_run": skipped}), flush=True)
+        del g, want
         torch.cuda.empty_cache()
 
 
