@@ -158,6 +158,7 @@ int plan_launch(const bw_context *ctx, int variant, bool side, const bw_launch_c
     } else if (variant >= 16 && variant < 32) {
         l.k = bfs_vertex_kernel(variant / 4, variant % 4, side);
         const int fam = variant / 4;
+        if (fam == 4 || fam == 6) l.k2 = bfs_hub_kernel(side);   // vertex-push(-warp): hub rows in chunks
         if (fam == 6 || fam == 7) {
             // ImplementationTemplate.hpp:463-471: power-of-two W <= 32, C % W == 0
             if (W == 0 || W > 32 || (W & (W - 1)) || C == 0 || C % W) return BW_ERR_INVALID_ARGUMENT;
@@ -211,7 +212,8 @@ BfsArgs make_args(bw_context *ctx, const bw_graph_view *g, int32_t *levels, int3
 int launch(const Launch &l, const BfsArgs &a, cudaStream_t s)
 {
     l.k<<<l.grid, l.block, l.smem, s>>>(a);
-    if (l.k2) l.k2<<<l.grid, l.block, 0, s>>>(a);
+    // the hub-chunk kernel is built for 256-thread blocks: the same threads
+    if (l.k2) l.k2<<<hub_grid(l.grid, l.block), 256, 0, s>>>(a);
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
@@ -370,7 +372,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
                 bfs_cluster_kernel(side)<<<CLUSTER_CTAS, CLUSTER_THREADS, 0, cap>>>(a);
             }
             plan.k<<<plan.grid, plan.block, plan.smem, cap>>>(a);
-            if (plan.k2) plan.k2<<<plan.grid, plan.block, 0, cap>>>(a);
+            if (plan.k2) plan.k2<<<hub_grid(plan.grid, plan.block), 256, 0, cap>>>(a);
             k_bfs_step<<<1, 32, 0, cap>>>(ctx->bfs_ctl, log, log_cap, handle);
             cudaGraph_t captured = body;
             e = cudaStreamEndCapture(cap, &captured);

@@ -203,6 +203,18 @@ __global__ void __launch_bounds__(512) k_bfs_edge(BfsArgs a)
 // ---------------------------------------------------------------------------
 constexpr uint32_t BFS_PUSH_HEAVY = 32;
 constexpr int BFS_PUSH_UNROLL = 8;
+// Rows above BFS_PUSH_GIANT edges are cut into HUB_CHUNK chunks for
+// k_bfs_hub_chunks (the level's second kernel), as frontier-push does: one
+// warp expanding a hub of R-MAT's lowest ids would hold the level.
+constexpr uint32_t BFS_PUSH_GIANT = 1024;
+
+__device__ __forceinline__ void queue_hub_chunks(const BfsArgs &a, LevelSlot *slot, uint32_t v, uint32_t s,
+                                                 uint32_t e)
+{
+    const uint32_t chunks = (e - s + HUB_CHUNK - 1) / HUB_CHUNK;
+    const uint32_t base = atomicAdd(&slot->heavy, chunks);
+    for (uint32_t c = 0; c < chunks; c++) a.heavy[base + c] = make_uint2(v, s + c * HUB_CHUNK);
+}
 
 // Relaxes the neighbours E[first + k * step] (k < BFS_PUSH_UNROLL, below
 // `end`): their indices, then their depths, are all in flight before the
@@ -243,9 +255,11 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
     auto relax_batch = [&](uint32_t first, uint32_t step, uint32_t end) {
         relax_neighbours(a, a.fwd_e, lv, nd, first, step, end, cnt, side, qnext, slot);
     };
-    auto expand = [&](uint32_t s, uint32_t e) {
-        const bool heavy = e - s > BFS_PUSH_HEAVY;
-        if (!heavy)
+    auto expand = [&](uint32_t v, uint32_t s, uint32_t e) {
+        const bool giant = e - s > BFS_PUSH_GIANT;
+        if (giant) queue_hub_chunks(a, slot, v, s, e);
+        const bool heavy = !giant && e - s > BFS_PUSH_HEAVY;
+        if (!heavy && !giant)
             for (uint32_t i = s; i < e; i += BFS_PUSH_UNROLL) relax_batch(i, 1, e);
         for (unsigned hv = __ballot_sync(FULL_MASK, heavy); hv; hv &= hv - 1) {
             const unsigned l = __ffs(hv) - 1;
@@ -266,7 +280,7 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
                 s = a.fwd_v[4 * g + k];
                 e = a.fwd_v[4 * g + k + 1];
             }
-            expand(s, e);
+            expand(static_cast<uint32_t>(4 * g + k), s, e);
         }
     }
     for (uint64_t v0 = (groups << 2) + gtid() - lane; v0 < n; v0 += stride) {
@@ -276,7 +290,7 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
             s = a.fwd_v[v];
             e = a.fwd_v[v + 1];
         }
-        expand(s, e);
+        expand(static_cast<uint32_t>(v), s, e);
     }
     cnt.finish(&slot->frontier);
     side.finish(slot);
@@ -372,9 +386,14 @@ __global__ void __launch_bounds__(512) k_bfs_vwarp(BfsArgs a)
         for (uint32_t v = 0; v < cntv; v++) {
             const uint32_t s = my_off[v], e = my_off[v + 1];
             if constexpr (!PULL) {
-                if (my_lv[v] == depth)
-                    for (uint32_t base = s; base < e; base += W * BFS_PUSH_UNROLL)
-                        relax_neighbours(a, E, lv, nd, base + lane, W, e, cnt, side, qnext, slot);
+                if (my_lv[v] == depth) {
+                    if (e - s > BFS_PUSH_GIANT) {             // to k_bfs_hub_chunks
+                        if (lane == 0) queue_hub_chunks(a, slot, static_cast<uint32_t>(v0 + v), s, e);
+                    } else {
+                        for (uint32_t base = s; base < e; base += W * BFS_PUSH_UNROLL)
+                            relax_neighbours(a, E, lv, nd, base + lane, W, e, cnt, side, qnext, slot);
+                    }
+                }
             } else {
                 if (my_lv[v] > depth) {
                     bool found = false;

@@ -150,6 +150,10 @@ BfsKernelFn bfs_edge_kernel(int layout, int reduction, bool side);
 BfsKernelFn bfs_vertex_kernel(int family, int reduction, bool side);
 BfsKernelFn bfs_frontier_push_kernel(bool side);
 BfsKernelFn bfs_hub_kernel(bool side);
+// The hub-chunk kernel runs 256-thread blocks: the grid that gives it the
+// same number of threads as a level kernel of `grid` x `block`.
+inline unsigned hub_grid(unsigned grid, unsigned block)
+{ return static_cast<unsigned>((static_cast<unsigned long long>(grid) * block + 255) / 256); }
 BfsKernelFn bfs_frontier_pull_kernel(bool side);
 BfsKernelFn bfs_cluster_kernel(bool side);   // 8-CTA cluster, CLUSTER_CTAS blocks of 1024 threads
 constexpr unsigned CLUSTER_CTAS = 8;

@@ -573,7 +573,7 @@ int bw_bfs_profile(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32
     auto run_one = [&](uint32_t k) {
         BfsArgs a = bfs_args(ctx, g, levels, static_cast<int32_t>(L), nullptr);
         plans[k].k<<<plans[k].grid, plans[k].block, plans[k].smem, s>>>(a);
-        if (plans[k].k2) plans[k].k2<<<plans[k].grid, plans[k].block, 0, s>>>(a);
+        if (plans[k].k2) plans[k].k2<<<hub_grid(plans[k].grid, plans[k].block), 256, 0, s>>>(a);
     };
     for (; L < max_levels; L++) {
         float lmax;
@@ -668,7 +668,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             const int c = pick(probs, K, sw->fallback, sw->threshold);
             BfsArgs a = bfs_args(ctx, g, levels, static_cast<int32_t>(L), nullptr);
             plans[c].k<<<plans[c].grid, plans[c].block, plans[c].smem, s>>>(a);
-            if (plans[c].k2) plans[c].k2<<<plans[c].grid, plans[c].block, 0, s>>>(a);
+            if (plans[c].k2) plans[c].k2<<<hub_grid(plans[c].grid, plans[c].block), 256, 0, s>>>(a);
             BW_CUDA(cudaGetLastError());
             BW_CUDA(cudaMemcpyAsync(&ctx->bfs_ctl_host->slot[L % 3], &ctx->bfs_ctl->slot[L % 3], sizeof(LevelSlot),
                                     cudaMemcpyDeviceToHost, s));
