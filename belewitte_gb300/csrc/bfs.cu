@@ -330,7 +330,10 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
     Launch plan;
     BW_TRY(plan_launch(ctx, variant, side, cfg, &plan));
     const bool cluster_path = variant == V_FRONTIER_PUSH;
-    if (cluster_path) BW_TRY(ensure_outdeg(ctx, g, s));   // frontier edge volumes gate the cluster path
+    if (cluster_path) {
+        BW_TRY(ensure_outdeg(ctx, g, s));   // frontier edge volumes gate the cluster path
+        BW_TRY(bfs_cluster_prepare());
+    }
     LevelSlot *log = nullptr;
     const uint32_t log_cap = stats ? std::min(stats_cap, max_levels) : 0;
     if (log_cap) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
@@ -369,7 +372,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
                 a.skip_check = 1;
                 a.log = log;
                 a.log_cap = log_cap;
-                bfs_cluster_kernel(side)<<<CLUSTER_CTAS, CLUSTER_THREADS, 0, cap>>>(a);
+                bfs_cluster_kernel(side)<<<CLUSTER_CTAS, CLUSTER_THREADS, bfs_cluster_smem(), cap>>>(a);
             }
             plan.k<<<plan.grid, plan.block, plan.smem, cap>>>(a);
             if (plan.k2) plan.k2<<<hub_grid(plan.grid, plan.block), 256, 0, cap>>>(a);

@@ -590,140 +590,146 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
 
 // ---------------------------------------------------------------------------
 // frontier-push, small-frontier path (device loop only): one cluster of
-// CLUSTER_CTAS blocks keeps expanding levels, separated by cluster barriers,
-// while the frontier stays at or below CLUSTER_CAP vertices -- the
-// high-diameter case (2-D grids, BFS tails) where one launch per level would
-// dominate.  It does the per-level bookkeeping of the device-loop step for
-// every level but the last, sets ctl->skip so the regular frontier-push
-// kernels of the same loop iteration return at once, and leaves the last
-// level to the step kernel.  A frontier above the cap at entry is left to
-// the regular kernels.  Data written by other CTAs of the cluster (queues,
-// hub chunks, counters) is read through L2 (L1 is not coherent).
+// CLUSTER_CTAS blocks keeps expanding levels while the frontier stays small
+// -- the high-diameter case (2-D grids, BFS tails) where one launch per
+// level would dominate.  A level is then a short chain of dependent
+// accesses, so the kernel keeps all else on chip:
+//  * each block holds a share of the frontier in shared memory as
+//    {vertex, row start, row end}: a level reads no queue and no offsets
+//    from global memory;
+//  * a neighbour is claimed with one atomicMin on its depth; the winner
+//    loads the neighbour's row bounds into its block's next list;
+//  * after the level's one cluster barrier, every block reads the blocks'
+//    counts and then its equal share of the next frontier from the other
+//    blocks' shared memory (a wavefront found by one block would otherwise
+//    stay with it).  The next lists alternate between two buffers, so the
+//    copy needs no second barrier.
+// Rows above CLUSTER_HEAVY edges are left to the full-GPU kernels (their
+// hub chunks spread such a row over every SM): a frontier with one is not
+// taken on, and a level that finds one hands over.  So do a frontier above
+// the caps and a block list overflow (the overflow went to the global queue
+// already): the blocks write their lists to the global queue after the
+// overflow, the leader fills the level's slot as the regular kernels would
+// have, sets ctl->skip so that the regular frontier-push kernels of the loop
+// iteration return at once, and leaves that level's bookkeeping to the step
+// kernel.  The leader does the bookkeeping of the levels it completes.
 // ---------------------------------------------------------------------------
-constexpr uint32_t CLUSTER_CAP = 65536;            // frontier vertices
-constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;   // frontier out-edges
-constexpr uint32_t CLUSTER_STAGE = 8192;           // next-frontier entries staged per block
+constexpr uint32_t CLUSTER_LIST = 4096;            // frontier entries per block list
+constexpr uint32_t CLUSTER_CAP = CLUSTER_LIST * CLUSTER_CTAS;   // frontier vertices
+constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;        // frontier out-edges
+constexpr uint32_t CLUSTER_HEAVY = 1024;           // rows above: the full-GPU kernels
+constexpr int CLUSTER_UNROLL = 4;
+static_assert(CLUSTER_THREADS == 32 * 32, "the block's counts are reduced by one warp, one lane per warp");
+// dynamic shared memory: the level's share and two next lists, each of
+// {vertex, row start, row end}
+constexpr size_t CLUSTER_SMEM = 3 * 3 * CLUSTER_LIST * sizeof(uint32_t);
 
-// Per-level accumulators of one block of the cluster kernel: every thread
-// counts locally, the block reduces once per level and issues one global
-// atomic per counter (per-warp atomics on the shared level slot serialise
-// at L2 and dominated short levels).  Newly visited vertices are staged in
-// shared memory and copied to the global next-frontier queue in one block
-// once the level is done; entries beyond the stage go to the queue directly.
-template<bool SIDE>
-struct ClusterLevel {
-    uint32_t hits = 0;
-    unsigned long long fe = 0;
-    float ls = 0.f, lq = 0.f, lm = 0.f;
-
-    __device__ __forceinline__ void visit(const BfsArgs &a, uint32_t *stage, uint32_t *stage_n, uint32_t *qnext,
-                                          LevelSlot *slot, uint32_t v)
-    {
-        hits++;
-        cg::coalesced_group g = cg::coalesced_threads();
-        uint32_t base = 0;
-        if (g.thread_rank() == 0) base = atomicAdd(stage_n, g.size());
-        base = g.shfl(base, 0) + g.thread_rank();
-        if (base < CLUSTER_STAGE) stage[base] = v;
-        else queue_append(qnext, &slot->qlen, v);
-        const uint32_t d = a.outdeg[v];
-        fe += d;
-        if constexpr (SIDE) {
-            const float l = __log2f(1.0f + static_cast<float>(d));
-            ls += l; lq += l * l; lm = fmaxf(lm, l);
-        }
-    }
-
-    // Every thread of the block calls; ends with the staged entries in the
-    // global queue and the level's counters in `slot`.
-    __device__ __forceinline__ void finish(uint32_t *stage, uint32_t *stage_n, uint32_t *qnext, LevelSlot *slot)
-    {
-        __shared__ unsigned long long r_fe[CLUSTER_THREADS / 32];
-        __shared__ uint32_t r_hits[CLUSTER_THREADS / 32];
-        __shared__ float r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32], r_lm[CLUSTER_THREADS / 32];
-        __shared__ uint32_t q_base;
-        const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        for (int o = 16; o > 0; o >>= 1) {
-            hits += __shfl_xor_sync(FULL_MASK, hits, o);
-            fe += __shfl_xor_sync(FULL_MASK, fe, o);
-            if constexpr (SIDE) {
-                ls += __shfl_xor_sync(FULL_MASK, ls, o);
-                lq += __shfl_xor_sync(FULL_MASK, lq, o);
-                lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
-            }
-        }
-        if (lane == 0) { r_hits[wid] = hits; r_fe[wid] = fe; r_ls[wid] = ls; r_lq[wid] = lq; r_lm[wid] = lm; }
-        __syncthreads();
-        const uint32_t staged = min(*stage_n, CLUSTER_STAGE);
-        if (threadIdx.x == 0) {
-            uint32_t h = 0;
-            unsigned long long e = 0;
-            float s1 = 0.f, s2 = 0.f, mx = 0.f;
-            for (unsigned w = 0; w < CLUSTER_THREADS / 32; w++) {
-                h += r_hits[w]; e += r_fe[w]; s1 += r_ls[w]; s2 += r_lq[w]; mx = fmaxf(mx, r_lm[w]);
-            }
-            if (h) atomicAdd(&slot->frontier, h);
-            if (e) atomicAdd(&slot->fedges, e);
-            if constexpr (SIDE) {
-                if (h) {
-                    atomicAdd(&slot->lsum, s1);
-                    atomicAdd(&slot->lsq, s2);
-                    atomicMax(&slot->lmax_bits, __float_as_uint(mx));
-                }
-            }
-            q_base = staged ? atomicAdd(&slot->qlen, staged) : 0u;
-        }
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < staged; i += blockDim.x) qnext[q_base + i] = stage[i];
-        hits = 0; fe = 0; ls = lq = lm = 0.f;
-    }
+struct ClusterCounts {
+    uint32_t frontier;            // new vertices of the level found by this block
+    uint32_t listed;              // of those, in the block's next list
+    unsigned long long fedges;    // their out-edges
+    float ls, lq, lm;             // log-degree statistics (SIDE)
+    uint32_t heavy;               // of those, rows above CLUSTER_HEAVY
 };
 
 template<bool SIDE>
 __global__ void __cluster_dims__(CLUSTER_CTAS, 1, 1) __launch_bounds__(CLUSTER_THREADS)
 k_bfs_cluster(BfsArgs a)
 {
+    extern __shared__ uint32_t cl_lists[];
     __shared__ uint32_t s_excl[CLUSTER_THREADS / 32][32];
     __shared__ uint32_t s_start[CLUSTER_THREADS / 32][32];
-    __shared__ uint32_t s_stage[CLUSTER_STAGE];
-    __shared__ uint32_t s_stage_n;
+    __shared__ ClusterCounts s_cnt[2];             // by level parity; read by the other blocks
+    __shared__ ClusterCounts s_tot;                // the cluster's totals
+    __shared__ uint32_t s_pre[CLUSTER_CTAS + 1];    // exclusive prefix of the blocks' next lists
+    __shared__ unsigned long long r_fe[CLUSTER_THREADS / 32];
+    __shared__ uint32_t r_hits[CLUSTER_THREADS / 32], r_heavy[CLUSTER_THREADS / 32];
+    __shared__ float r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32], r_lm[CLUSTER_THREADS / 32];
+    __shared__ uint32_t s_n, s_cur_n;
     cg::cluster_group cl = cg::this_cluster();
     BfsCtl *ctl = a.ctl;
-    const unsigned rank = cl.block_rank();
-    const bool leader = rank == 0 && threadIdx.x == 0;
+    const unsigned rank = cl.block_rank(), tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+    const bool leader = rank == 0 && tid == 0;
     int32_t L = *((volatile int32_t *) &ctl->depth);
     const uint32_t max_levels = *((volatile uint32_t *) &ctl->max_levels);
-    uint32_t qlen = *((volatile uint32_t *) &ctl->slot[(L + 2) % 3].qlen);
+    const uint32_t qlen = *((volatile uint32_t *) &ctl->slot[(L + 2) % 3].qlen);
     const unsigned long long fedges = *((volatile unsigned long long *) &ctl->slot[(L + 2) % 3].fedges);
     // same values in every block: a large or edge-heavy frontier is left to
     // the full-GPU kernels
     if (qlen == 0 || qlen > CLUSTER_CAP || fedges > CLUSTER_EDGE_CAP) return;
     int32_t *lv = a.levels;
-    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint64_t warp = uint64_t(rank) * (CLUSTER_THREADS / 32) + wib;
-    const uint64_t warps = uint64_t(CLUSTER_CTAS) * (CLUSTER_THREADS / 32);
-    ClusterLevel<SIDE> acc;
+    // buffer 0: the level's share; buffers 1 and 2: next lists, alternating
+    uint32_t *lst_v[3], *lst_s[3], *lst_e[3];
+    for (int b = 0; b < 3; b++) {
+        lst_v[b] = cl_lists + (3 * b) * CLUSTER_LIST;
+        lst_s[b] = cl_lists + (3 * b + 1) * CLUSTER_LIST;
+        lst_e[b] = cl_lists + (3 * b + 2) * CLUSTER_LIST;
+    }
+    {   // this block's share of the level's queue, with the rows' bounds
+        const uint32_t *qin = (L & 1) ? a.q1 : a.q0;
+        const uint32_t per = (qlen + CLUSTER_CTAS - 1) / CLUSTER_CTAS;
+        const uint32_t b = min(qlen, rank * per), cnt = min(per, qlen - b);   // cnt <= CLUSTER_LIST
+        uint32_t heavy = 0;
+        for (uint32_t i = tid; i < cnt; i += CLUSTER_THREADS) {
+            const uint32_t v = __ldcg(qin + b + i);
+            const uint32_t rs = a.fwd_v[v], re = a.fwd_v[v + 1];
+            lst_v[0][i] = v;
+            lst_s[0][i] = rs;
+            lst_e[0][i] = re;
+            heavy |= re - rs > CLUSTER_HEAVY ? 1u : 0u;
+        }
+        heavy = __syncthreads_or(heavy);
+        if (tid == 0) {
+            s_cur_n = cnt;
+            s_cnt[1].heavy = heavy;
+        }
+        cl.sync();
+        uint32_t any = 0;
+        if (tid < CLUSTER_CTAS) any = cl.map_shared_rank(&s_cnt[1], tid)->heavy;
+        any = __syncthreads_or(any);
+        cl.sync();                                   // nobody leaves while its flag may be read
+        if (any) return;                             // a hub row: the full-GPU kernels take this level
+    }
+    int p = 0;                                       // next lists: buffer 1 + p
     for (;;) {
         const int32_t nd = L + 1;
         LevelSlot *slot = &ctl->slot[L % 3];
-        if (leader) reset_slot(&ctl->slot[(L + 1) % 3]);
-        if (threadIdx.x == 0) s_stage_n = 0;
-        __syncthreads();
-        const uint32_t *qin = (L & 1) ? a.q1 : a.q0;
         uint32_t *qnext = (L & 1) ? a.q0 : a.q1;
-        for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
-            const uint64_t i = t + lane;
-            uint32_t v = 0, s = 0, d = 0;
-            if (i < qlen) {
-                v = __ldcg(qin + i);
-                s = a.fwd_v[v];
-                d = a.fwd_v[v + 1] - s;
+        if (leader) reset_slot(&ctl->slot[(L + 1) % 3]);
+        if (tid == 0) s_n = 0;
+        __syncthreads();
+        const uint32_t ncur = s_cur_n;
+        const uint32_t *cs = lst_s[0], *ce = lst_e[0];
+        uint32_t *nv = lst_v[1 + p], *ns = lst_s[1 + p], *ne = lst_e[1 + p];
+        uint32_t hits = 0, heavy = 0;
+        unsigned long long fe = 0;
+        float ls = 0.f, lq = 0.f, lm = 0.f;
+        auto claim = [&](uint32_t u) {
+            if (atomicMin(&lv[u], nd) <= nd) return;
+            const uint32_t us = a.fwd_v[u], ue = a.fwd_v[u + 1];
+            hits++;
+            fe += ue - us;
+            heavy += ue - us > CLUSTER_HEAVY ? 1u : 0u;
+            if constexpr (SIDE) {
+                const float l = __log2f(1.0f + static_cast<float>(ue - us));
+                ls += l; lq += l * l; lm = fmaxf(lm, l);
             }
-            if (d > HEAVY_DEGREE) {
-                const uint32_t chunks = (d + HUB_CHUNK - 1) / HUB_CHUNK;
-                const uint32_t base = atomicAdd(&slot->heavy, chunks);
-                for (uint32_t c = 0; c < chunks; c++) a.heavy[base + c] = make_uint2(v, s + c * HUB_CHUNK);
-                d = 0;
+            const uint32_t k = atomicAdd(&s_n, 1u);
+            if (k < CLUSTER_LIST) {
+                nv[k] = u;
+                ns[k] = us;
+                ne[k] = ue;
+            } else {                                     // overflow: straight to the global queue
+                qnext[atomicAdd(&slot->qlen, 1u)] = u;
+            }
+        };
+        // 32 entries per warp step, their rows concatenated
+        for (uint32_t t = wib * 32; t < ncur; t += CLUSTER_THREADS) {
+            const uint32_t i = t + lane;
+            uint32_t s = 0, d = 0;
+            if (i < ncur) {
+                s = cs[i];
+                d = ce[i] - s;
             }
             uint32_t incl = d;
             for (int o = 1; o < 32; o <<= 1) {
@@ -734,56 +740,131 @@ k_bfs_cluster(BfsArgs a)
             s_excl[wib][lane] = incl - d;
             s_start[wib][lane] = s;
             __syncwarp();
-            for (uint32_t k = lane; k < total; k += 32) {
-                int lo = 0, hi = 31;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
+            uint32_t seg = 0;
+            for (uint32_t k0 = 0; k0 < total; k0 += 32 * CLUSTER_UNROLL) {
+                uint32_t u[CLUSTER_UNROLL];
+#pragma unroll
+                for (int jj = 0; jj < CLUSTER_UNROLL; jj++) {
+                    const uint32_t k = k0 + jj * 32 + lane;
+                    u[jj] = 0xffffffffu;
+                    if (k < total) {
+                        while (seg < 31 && s_excl[wib][seg + 1] <= k) seg++;
+                        u[jj] = __ldg(a.fwd_e + s_start[wib][seg] + (k - s_excl[wib][seg]));
+                    }
                 }
-                const uint32_t u = __ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo]));
-                if (relax(lv, u, nd)) acc.visit(a, s_stage, &s_stage_n, qnext, slot, u);
+#pragma unroll
+                for (int jj = 0; jj < CLUSTER_UNROLL; jj++)
+                    if (u[jj] != 0xffffffffu) claim(u[jj]);
             }
             __syncwarp();
         }
-        acc.finish(s_stage, &s_stage_n, qnext, slot);
-        cl.sync();
-        const uint32_t chunks = __ldcg(&slot->heavy);
-        if (chunks) {                                      // hub chunks: a second phase
-            if (threadIdx.x == 0) s_stage_n = 0;
-            __syncthreads();
-            for (uint64_t c = warp; c < chunks; c += warps) {
-                const uint2 h = __ldcg(a.heavy + c);
-                const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
-                for (uint32_t i = h.y + lane; i < end; i += 32) {
-                    const uint32_t u = __ldg(a.fwd_e + i);
-                    if (relax(lv, u, nd)) acc.visit(a, s_stage, &s_stage_n, qnext, slot, u);
-                }
+        // the block's counts
+        for (int o = 16; o > 0; o >>= 1) {
+            hits += __shfl_xor_sync(FULL_MASK, hits, o);
+            heavy += __shfl_xor_sync(FULL_MASK, heavy, o);
+            fe += __shfl_xor_sync(FULL_MASK, fe, o);
+            if constexpr (SIDE) {
+                ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
             }
-            acc.finish(s_stage, &s_stage_n, qnext, slot);
-            cl.sync();
         }
-        const uint32_t f = __ldcg(&slot->qlen);
-        const unsigned long long fnext = __ldcg(&slot->fedges);
-        if (f == 0 || f > CLUSTER_CAP || fnext > CLUSTER_EDGE_CAP || static_cast<uint32_t>(L) + 2 > max_levels) {
-            if (leader) ctl->skip = 1;                     // level L is left to the step kernel
+        if (lane == 0) {
+            r_hits[wib] = hits; r_heavy[wib] = heavy; r_fe[wib] = fe;
+            r_ls[wib] = ls; r_lq[wib] = lq; r_lm[wib] = lm;
+        }
+        __syncthreads();
+        if (wib == 0) {                                  // the block's totals: one warp, in parallel
+            ClusterCounts c{};
+            c.frontier = r_hits[lane]; c.heavy = r_heavy[lane]; c.fedges = r_fe[lane];
+            c.ls = r_ls[lane]; c.lq = r_lq[lane]; c.lm = r_lm[lane];
+            for (int o = 16; o > 0; o >>= 1) {
+                c.frontier += __shfl_xor_sync(FULL_MASK, c.frontier, o);
+                c.heavy += __shfl_xor_sync(FULL_MASK, c.heavy, o);
+                c.fedges += __shfl_xor_sync(FULL_MASK, c.fedges, o);
+                c.ls += __shfl_xor_sync(FULL_MASK, c.ls, o);
+                c.lq += __shfl_xor_sync(FULL_MASK, c.lq, o);
+                c.lm = fmaxf(c.lm, __shfl_xor_sync(FULL_MASK, c.lm, o));
+            }
+            c.listed = min(s_n, CLUSTER_LIST);
+            if (lane == 0) s_cnt[p] = c;
+        }
+        cl.sync();                                       // every block's counts, list and overflow are out
+        if (wib == 0) {                                  // the cluster's totals, read by one warp
+            ClusterCounts c{};
+            if (lane < CLUSTER_CTAS) c = *cl.map_shared_rank(&s_cnt[p], lane);
+            uint32_t incl = c.listed;                    // prefix of the lists over ranks
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
+                if (lane >= static_cast<unsigned>(o)) incl += y;
+            }
+            if (lane < CLUSTER_CTAS) s_pre[lane + 1] = incl;
+            if (lane == 0) s_pre[0] = 0;
+            for (int o = 16; o > 0; o >>= 1) {
+                c.frontier += __shfl_xor_sync(FULL_MASK, c.frontier, o);
+                c.listed += __shfl_xor_sync(FULL_MASK, c.listed, o);
+                c.heavy += __shfl_xor_sync(FULL_MASK, c.heavy, o);
+                c.fedges += __shfl_xor_sync(FULL_MASK, c.fedges, o);
+                c.ls += __shfl_xor_sync(FULL_MASK, c.ls, o);
+                c.lq += __shfl_xor_sync(FULL_MASK, c.lq, o);
+                c.lm = fmaxf(c.lm, __shfl_xor_sync(FULL_MASK, c.lm, o));
+            }
+            if (lane == 0) s_tot = c;
+        }
+        __syncthreads();
+        const uint32_t f = s_tot.frontier, listed_all = s_tot.listed;
+        const unsigned long long fe_all = s_tot.fedges;
+        const float ls_all = s_tot.ls, lq_all = s_tot.lq, lm_all = s_tot.lm;
+        if (f == 0 || f > CLUSTER_CAP || fe_all > CLUSTER_EDGE_CAP || listed_all < f || s_tot.heavy ||
+            static_cast<uint32_t>(L) + 2 > max_levels) {
+            // hand level L to the step kernel: the next queue (overflow first,
+            // then the blocks' lists) and the level's slot
+            const uint32_t at = (f - listed_all) + s_pre[rank], mine = s_cnt[p].listed;
+            for (uint32_t i = tid; i < mine; i += CLUSTER_THREADS) qnext[at + i] = nv[i];
+            if (leader) {
+                slot->frontier = f;
+                slot->qlen = f;
+                slot->fedges = fe_all;
+                slot->lsum = ls_all;
+                slot->lsq = lq_all;
+                slot->lmax_bits = __float_as_uint(lm_all);
+                slot->heavy = 0;
+                ctl->skip = 1;
+            }
+            cl.sync();                                   // no block leaves while others may read its counts
             return;
         }
         if (leader) {                                      // the step kernel's bookkeeping for level L
             LevelSlot sl;
-            sl.frontier = __ldcg(&slot->frontier);
+            sl.frontier = f;
             sl.qlen = f;
-            sl.fedges = __ldcg(&slot->fedges);
-            sl.lsum = __ldcg(&slot->lsum);
-            sl.lsq = __ldcg(&slot->lsq);
-            sl.lmax_bits = __ldcg(&slot->lmax_bits);
+            sl.fedges = fe_all;
+            sl.lsum = ls_all;
+            sl.lsq = lq_all;
+            sl.lmax_bits = __float_as_uint(lm_all);
             sl.heavy = static_cast<uint32_t>(ctl->variant);
             if (a.log && static_cast<uint32_t>(L) < a.log_cap) a.log[L] = sl;
-            ctl->visited += sl.frontier;
-            ctl->traversed += sl.fedges;
+            ctl->visited += f;
+            ctl->traversed += fe_all;
             ctl->levels_done = static_cast<uint32_t>(L) + 1;
             ctl->depth = L + 1;
         }
-        qlen = f;
+        // this block's equal share of the next frontier, gathered from the
+        // blocks' next lists (rank order) into the level buffer
+        {
+            const uint32_t per = (f + CLUSTER_CTAS - 1) / CLUSTER_CTAS;
+            const uint32_t b = min(f, rank * per), cnt = min(per, f - b);
+            for (uint32_t i = tid; i < cnt; i += CLUSTER_THREADS) {
+                const uint32_t j = b + i;
+                unsigned q = 0;
+                while (q + 1 < CLUSTER_CTAS && s_pre[q + 1] <= j) q++;
+                const uint32_t k = j - s_pre[q];
+                lst_s[0][i] = *cl.map_shared_rank(ns + k, q);
+                lst_e[0][i] = *cl.map_shared_rank(ne + k, q);
+            }
+            if (tid == 0) s_cur_n = cnt;
+        }
+        p ^= 1;
         L++;
     }
 }

@@ -35,6 +35,17 @@ BfsKernelFn bfs_hub_kernel(bool side)
 BfsKernelFn bfs_cluster_kernel(bool side)
 { return side ? k_bfs_cluster<true> : k_bfs_cluster<false>; }
 
+size_t bfs_cluster_smem() { return CLUSTER_SMEM; }
+
+int bfs_cluster_prepare()
+{
+    BW_CUDA(cudaFuncSetAttribute(k_bfs_cluster<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(CLUSTER_SMEM)));
+    BW_CUDA(cudaFuncSetAttribute(k_bfs_cluster<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(CLUSTER_SMEM)));
+    return BW_OK;
+}
+
 BfsKernelFn bfs_frontier_pull_kernel(bool side)
 { return side ? k_bfs_frontier_pull<true> : k_bfs_frontier_pull<false>; }
 

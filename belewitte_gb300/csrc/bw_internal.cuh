@@ -156,6 +156,8 @@ inline unsigned hub_grid(unsigned grid, unsigned block)
 { return static_cast<unsigned>((static_cast<unsigned long long>(grid) * block + 255) / 256); }
 BfsKernelFn bfs_frontier_pull_kernel(bool side);
 BfsKernelFn bfs_cluster_kernel(bool side);   // 8-CTA cluster, CLUSTER_CTAS blocks of 1024 threads
+size_t bfs_cluster_smem();                    // its dynamic shared memory
+int bfs_cluster_prepare();                    // allows that much on the current device
 constexpr unsigned CLUSTER_CTAS = 8;
 constexpr unsigned CLUSTER_THREADS = 1024;
 

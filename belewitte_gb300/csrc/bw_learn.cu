@@ -695,6 +695,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
     if (loop_mode != BW_LOOP_GRAPH) return BW_ERR_INVALID_ARGUMENT;
 
     // Device loop: WHILE { predict -> SWITCH(K level bodies) -> step }.
+    BW_TRY(bfs_cluster_prepare());          // frontier-push's small-frontier kernel, if a candidate
     LevelSlot *log = nullptr;
     const uint32_t log_cap = stats ? std::min(stats_cap, max_levels) : 0;
     if (log_cap) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&log), log_cap * sizeof(LevelSlot), s));
@@ -755,6 +756,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
                 cp.func = reinterpret_cast<void *>(bfs_cluster_kernel(true));
                 cp.gridDim = dim3(CLUSTER_CTAS);
                 cp.blockDim = dim3(CLUSTER_THREADS);
+                cp.sharedMemBytes = static_cast<unsigned>(bfs_cluster_smem());
                 cp.kernelParams = kargs;
                 if ((e = cudaGraphAddKernelNode(&first, kb, nullptr, 0, &cp)) != cudaSuccess) { fail(e, "cluster node"); break; }
             }
@@ -771,6 +773,8 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             if (plans[k].k2) {
                 cudaKernelNodeParams lp2 = lp;
                 lp2.func = reinterpret_cast<void *>(plans[k].k2);
+                lp2.gridDim = dim3(hub_grid(plans[k].grid, plans[k].block));
+                lp2.blockDim = dim3(256);
                 lp2.sharedMemBytes = 0;
                 cudaGraphNode_t n2;
                 if ((e = cudaGraphAddKernelNode(&n2, kb, &n1, 1, &lp2)) != cudaSuccess) { fail(e, "hub node"); break; }

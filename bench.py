@@ -25,6 +25,7 @@ The same JSON line carries:
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --case pagerank:VARIANT:rmat22|er[:BLOCK:HUBS]   (small profiling case)
   python bench.py --case bfs:VARIANT:rmat22            (small profiling case)
+  python bench.py --case bfsgraph:VARIANT:grid          (device loop; the cluster kernel)
   python bench.py --sweep      (every PageRank variant on R-MAT-22 and ER, every BFS variant
                                 on R-MAT-24 sym, the grid and BA)
 
@@ -490,6 +491,9 @@ def run_case(spec: str):
         from belewitte_gb300 import learn
         root = int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item())
         learn.run_learned(ctx, g, learn.load_predictor(), root, loop="host", stats=False)
+    elif algo == "bfsgraph":
+        # device loop: small frontiers run in frontier-push's cluster kernel
+        bw.bfs(ctx, g, variant, int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item()), loop="graph")
     else:
         bw.bfs(ctx, g, variant, int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item()), loop="host")
     torch.cuda.synchronize()

@@ -130,3 +130,36 @@ def test_errors(ctx, graphs):
     # the context stays usable after errors
     run = bw.bfs(ctx, g, "vertex-push", r)
     assert np.array_equal(run.levels.cpu().numpy(), lv)
+
+
+def _two_stars(leaves):
+    """Root 0 -> hubs 1 and 2 -> `leaves` leaves each, then every leaf ->
+    one of 64 sinks: the frontier grows from 2 rows to 2 * leaves vertices
+    in one level (more than one block of the cluster kernel lists) and
+    shrinks again."""
+    n = 3 + 2 * leaves + 64
+    src = [0, 0]
+    dst = [1, 2]
+    for hub in (1, 2):
+        base = 3 + (hub - 1) * leaves
+        src += [hub] * leaves
+        dst += list(range(base, base + leaves))
+    lv = np.arange(3, 3 + 2 * leaves)
+    src += list(lv)
+    dst += list(3 + 2 * leaves + (lv % 64))
+    return bw.HostGraph.from_edges(n, np.array(src, np.uint32), np.array(dst, np.uint32))
+
+
+@pytest.mark.parametrize("leaves", [3000, 20000])
+def test_cluster_path_overflow(ctx, leaves):
+    """frontier-push's device loop keeps small frontiers in one cluster
+    launch; a level that discovers more vertices than a block's list holds
+    spills to the global queue and hands over to the full-GPU kernels.
+    Depths and per-level counts match the oracle either way."""
+    h = _two_stars(leaves)
+    g = bw.DeviceGraph(h)
+    want, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, 0)
+    for loop in ("graph", "host"):
+        run = bw.bfs(ctx, g, "frontier-push", 0, loop=loop, stats=True)
+        assert np.array_equal(run.levels.cpu().numpy(), want), loop
+        assert [s["frontier_vertices"] for s in run.level_stats] == list(cnt), loop
