@@ -33,6 +33,7 @@ constexpr float DAMPING = 0.85f;
 constexpr uint32_t BATCH_PR_LIGHT = 64;   // PageRank rows above this are summed by a whole warp
 constexpr int BATCH_PR_UNROLL = 8;
 constexpr int BATCH_BFS_UNROLL = 4;
+constexpr uint32_t BATCH_BU_DIV = 24;     // bottom-up levels: frontier above 1/24 of the unit
 constexpr uint32_t BATCH_PR_L = 8;        // warp sums: windows of 32 x 8 terms
 
 struct BatchArgs {
@@ -134,7 +135,50 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
                     qout[base + g.thread_rank()] = u;
                 }
             };
-            for (uint32_t t = wib * 32; t < len; t += BATCH_THREADS) {
+            // A frontier above 1/BATCH_BU_DIV of the unit's vertices: bottom-up.
+            // Every vertex not yet reached looks for an in-neighbour reached
+            // before this level, which is then at `depth` (one at a smaller
+            // depth would have reached it already); the bitmap answers, and
+            // is updated only once the level is done, so that it reads as of
+            // the level's start.
+            const uint32_t nunit = ve - vb;
+            const bool bottom_up = bitmap && a.rev_v && len > nunit / BATCH_BU_DIV;
+            if (bottom_up) {
+                const uint32_t words = (nunit + 31) / 32;
+                for (uint32_t w = tid; w < words; w += BATCH_THREADS) {
+                    uint32_t todo = ~s_vis[w];
+                    if (w == words - 1 && (nunit & 31)) todo &= (1u << (nunit & 31)) - 1u;
+                    while (todo) {
+                        const uint32_t v = vb + w * 32 + (__ffs(todo) - 1);
+                        todo &= todo - 1;
+                        const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
+                        bool found = false;
+                        for (uint32_t i = s; i < e && !found; i += BATCH_BFS_UNROLL) {
+                            uint32_t pu[BATCH_BFS_UNROLL];
+#pragma unroll
+                            for (int j = 0; j < BATCH_BFS_UNROLL; j++)
+                                pu[j] = i + j < e ? __ldg(a.rev_e + i + j) - vb : NO_UNIT;
+#pragma unroll
+                            for (int j = 0; j < BATCH_BFS_UNROLL; j++)
+                                if (pu[j] != NO_UNIT) found |= ((s_vis[pu[j] >> 5] >> (pu[j] & 31)) & 1u) != 0u;
+                        }
+                        if (found) {
+                            lv[v] = nd;
+                            cg::coalesced_group g = cg::coalesced_threads();
+                            uint32_t base = 0;
+                            if (g.thread_rank() == 0) base = atomicAdd(olen, g.size());
+                            base = g.shfl(base, 0);
+                            qout[base + g.thread_rank()] = v;
+                        }
+                    }
+                }
+                __syncthreads();
+                for (uint32_t i = tid; i < *olen; i += BATCH_THREADS) {
+                    const uint32_t u = qout[i] - vb;
+                    atomicOr(&s_vis[u >> 5], 1u << (u & 31));
+                }
+            }
+            for (uint32_t t = wib * 32; !bottom_up && t < len; t += BATCH_THREADS) {
                 const uint32_t i = t + lane;
                 uint32_t v = 0, s = 0, d = 0;
                 if (i < len) {
@@ -177,7 +221,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
                 __syncwarp();
             }
             __syncthreads();
-            const uint32_t heavy = min(s_heavy_n, HEAVY_SLOTS);
+            const uint32_t heavy = bottom_up ? 0u : min(s_heavy_n, HEAVY_SLOTS);
             for (uint32_t h = 0; h < heavy; h++) {
                 const uint32_t v = s_heavy[h];
                 const uint32_t s = a.fwd_v[v], e = a.fwd_v[v + 1];
