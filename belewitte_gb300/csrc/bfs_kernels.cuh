@@ -108,6 +108,70 @@ struct Side {
             }
         }
     }
+    // The same, one set of atomics per block (every thread of the block
+    // calls): the level's slot is one address per counter, and per-warp
+    // atomics from every warp of a large level serialise there.
+    __device__ __forceinline__ void finish_block(LevelSlot *s)
+    {
+        if constexpr (SIDE) {
+            __shared__ unsigned long long b_fe[32];
+            __shared__ float b_ls[32], b_lq[32], b_lm[32];
+            const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            for (int o = 16; o > 0; o >>= 1) {
+                fe += __shfl_xor_sync(FULL_MASK, fe, o);
+                ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+            }
+            if (lane == 0) { b_fe[wid] = fe; b_ls[wid] = ls; b_lq[wid] = lq; b_lm[wid] = lm; }
+            __syncthreads();
+            if (wid == 0) {
+                const bool in = lane < (blockDim.x >> 5);
+                fe = in ? b_fe[lane] : 0ull; ls = in ? b_ls[lane] : 0.f; lq = in ? b_lq[lane] : 0.f;
+                lm = in ? b_lm[lane] : 0.f;
+                for (int o = 16; o > 0; o >>= 1) {
+                    fe += __shfl_xor_sync(FULL_MASK, fe, o);
+                    ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                    lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                    lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+                }
+                if (lane == 0 && fe) {
+                    atomicAdd(&s->fedges, fe);
+                    atomicAdd(&s->lsum, ls);
+                    atomicAdd(&s->lsq, lq);
+                    atomicMax(&s->lmax_bits, __float_as_uint(lm));
+                }
+            }
+        }
+    }
+};
+
+// Next-queue appends staged per warp in shared memory: the whole warp calls
+// add() at a convergent point; a full stage goes to the queue with one
+// global atomic and coalesced stores.  One counter address takes every
+// append of a level, so a large level otherwise serialises on it.
+constexpr uint32_t WARP_STAGE = 256;
+struct WarpQueue {
+    uint32_t *stage;      // this warp's WARP_STAGE entries of shared memory
+    uint32_t n = 0;       // staged (warp-uniform)
+    __device__ __forceinline__ void add(bool hit, uint32_t v, uint32_t *q, uint32_t *len)
+    {
+        const unsigned lane = threadIdx.x & 31;
+        const unsigned m = __ballot_sync(FULL_MASK, hit);
+        if (hit) stage[n + __popc(m & ((1u << lane) - 1u))] = v;
+        n += __popc(m);
+        if (n > WARP_STAGE - 32) flush(q, len);
+    }
+    __device__ __forceinline__ void flush(uint32_t *q, uint32_t *len)
+    {
+        __syncwarp();
+        uint32_t base = 0;
+        if ((threadIdx.x & 31) == 0 && n) base = atomicAdd(len, n);
+        base = __shfl_sync(FULL_MASK, base, 0);
+        for (uint32_t i = threadIdx.x & 31; i < n; i += 32) q[base + i] = stage[i];
+        n = 0;
+        __syncwarp();
+    }
 };
 
 // Relax v to nd; true for exactly one caller per newly visited vertex.
@@ -436,6 +500,7 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
 {
     __shared__ uint32_t s_excl[8][32];
     __shared__ uint32_t s_start[8][32];
+    __shared__ uint32_t s_stage[8][WARP_STAGE];
     if (a.skip_check && *((volatile uint32_t *) &a.ctl->skip)) return;
     const int32_t depth = level_depth(a), nd = depth + 1;
     LevelSlot *slot = &a.ctl->slot[depth % 3];
@@ -444,11 +509,13 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
     uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
     const uint32_t qlen = *((volatile uint32_t *) &a.ctl->slot[(depth + 2) % 3].qlen);
     int32_t *lv = a.levels;
-    Counter<RED_WARP> cnt;
+    Counter<RED_BLOCK> cnt;
     Side<SIDE> side;
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
     unsigned long long fe = 0;   // next-frontier out-edges (cluster-path gating)
+    WarpQueue wq;
+    wq.stage = s_stage[wib];
 
     for (uint64_t t = warp * 32; t < qlen; t += warps * 32) {
         const uint64_t i = t + lane;
@@ -473,57 +540,73 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_push(BfsArgs a)
         s_excl[wib][lane] = incl - d;
         s_start[wib][lane] = s;
         __syncwarp();
-        for (uint32_t k = lane; k < total; k += 32) {
-            // owner = last lane with excl <= k
-            int lo = 0, hi = 31;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_excl[wib][mid] <= k) lo = mid; else hi = mid - 1;
+        // edge k of the concatenated rows: a per-lane cursor over the rows'
+        // exclusive offsets; whole-warp steps, so that the new vertices are
+        // staged with one ballot per step
+        uint32_t seg = 0;
+        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            bool got = false;
+            uint32_t u = 0;
+            if (k < total) {
+                while (seg < 31 && s_excl[wib][seg + 1] <= k) seg++;
+                u = __ldg(a.fwd_e + s_start[wib][seg] + (k - s_excl[wib][seg]));
+                got = relax(lv, u, nd);
             }
-            const uint32_t u = __ldg(a.fwd_e + s_start[wib][lo] + (k - s_excl[wib][lo]));
-            if (relax(lv, u, nd)) {
+            if (got) {
                 cnt.hit(&slot->frontier);
-                queue_append(qnext, &slot->qlen, u);
                 if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
                 else if (a.skip_check) fe += a.outdeg[u];
             }
+            wq.add(got, u, qnext, &slot->qlen);
         }
         __syncwarp();
     }
+    wq.flush(qnext, &slot->qlen);
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
     if constexpr (!SIDE) flush_edges(slot, fe);
 }
 
 template<bool SIDE>
 __global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
 {
+    __shared__ uint32_t s_stage[8][WARP_STAGE];
     if (a.skip_check && *((volatile uint32_t *) &a.ctl->skip)) return;
     const int32_t depth = level_depth(a), nd = depth + 1;
     LevelSlot *slot = &a.ctl->slot[depth % 3];
     uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
     const uint32_t chunks = *((volatile uint32_t *) &slot->heavy);
     int32_t *lv = a.levels;
-    Counter<RED_WARP> cnt;
+    Counter<RED_BLOCK> cnt;
     Side<SIDE> side;
     const unsigned lane = threadIdx.x & 31;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
     unsigned long long fe = 0;
+    WarpQueue wq;
+    wq.stage = s_stage[threadIdx.x >> 5];
     for (uint64_t c = warp; c < chunks; c += warps) {
         const uint2 h = a.heavy[c];
         const uint32_t end = min(h.y + HUB_CHUNK, a.fwd_v[h.x + 1]);
-        for (uint32_t i = h.y + lane; i < end; i += 32) {
-            const uint32_t u = __ldcs(a.fwd_e + i);
-            if (relax(lv, u, nd)) {
+        for (uint32_t i0 = h.y; i0 < end; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            bool got = false;
+            uint32_t u = 0;
+            if (i < end) {
+                u = __ldcs(a.fwd_e + i);
+                got = relax(lv, u, nd);
+            }
+            if (got) {
                 cnt.hit(&slot->frontier);
-                queue_append(qnext, &slot->qlen, u);
                 if constexpr (SIDE) side.visit(a, nullptr, nullptr, u);
                 else if (a.skip_check) fe += a.outdeg[u];
             }
+            wq.add(got, u, qnext, &slot->qlen);
         }
     }
+    wq.flush(qnext, &slot->qlen);
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
     if constexpr (!SIDE) flush_edges(slot, fe);
 }
 
@@ -537,17 +620,20 @@ __global__ void __launch_bounds__(256) k_bfs_hub_chunks(BfsArgs a)
 template<bool SIDE>
 __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
 {
+    __shared__ uint32_t s_stage[8][WARP_STAGE];
     const int32_t depth = level_depth(a), nd = depth + 1;
     LevelSlot *slot = &a.ctl->slot[depth % 3];
     if (blockIdx.x == 0 && threadIdx.x == 0) reset_slot(&a.ctl->slot[(depth + 1) % 3]);
     uint32_t *qnext = (depth & 1) ? a.q0 : a.q1;
     int32_t *lv = a.levels;
-    Counter<RED_WARP> cnt;
+    Counter<RED_BLOCK> cnt;
     Side<SIDE> side;
     const unsigned lane = threadIdx.x & 31;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
     const uint64_t n = a.n;
     constexpr uint32_t SOLO = 8;
+    WarpQueue wq;
+    wq.stage = s_stage[threadIdx.x >> 5];
 
     for (uint64_t t = warp * 32; t < n; t += warps * 32) {
         const uint64_t v = t + lane;
@@ -581,11 +667,13 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
         if (found) {
             lv[v] = nd;
             cnt.hit(&slot->frontier);
-            side.visit(a, qnext, slot, static_cast<uint32_t>(v));
+            side.visit(a, nullptr, slot, static_cast<uint32_t>(v));   // statistics; the queue below
         }
+        if constexpr (SIDE) wq.add(found, static_cast<uint32_t>(v), qnext, &slot->qlen);
     }
+    if constexpr (SIDE) wq.flush(qnext, &slot->qlen);
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
 }
 
 // ---------------------------------------------------------------------------
