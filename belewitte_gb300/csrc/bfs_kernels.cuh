@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(512) k_bfs_edge(BfsArgs a)
         else edge(a.rev_s[e].x, a.rev_s[e].y);
     }
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_push(BfsArgs a)
         expand(static_cast<uint32_t>(v), s, e);
     }
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -380,26 +380,35 @@ __global__ void __launch_bounds__(512) k_bfs_vertex_pull(BfsArgs a)
     int32_t *lv = a.levels;
     Counter<RED> cnt;
     Side<SIDE> side;
+    __shared__ uint32_t s_stage[SIDE ? 16 : 1][SIDE ? WARP_STAGE : 1];
+    WarpQueue wq;
+    wq.stage = s_stage[SIDE ? (threadIdx.x >> 5) : 0];
+    const unsigned lane = threadIdx.x & 31;
     const uint64_t n = a.n, stride = gthreads();
-    for (uint64_t v = gtid(); v < n; v += stride) {
-        if (lv[v] <= nd) continue;
-        const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
+    // whole-warp steps (the next queue is staged with one ballot per step)
+    for (uint64_t v0 = gtid() - lane; v0 < n; v0 += stride) {
+        const uint64_t v = v0 + lane;
         bool found = false;
-        for (uint32_t i = s; i < e && !found; i += BFS_PULL_UNROLL) {
-            uint32_t p[BFS_PULL_UNROLL];
+        if (v < n && lv[v] > nd) {
+            const uint32_t s = a.rev_v[v], e = a.rev_v[v + 1];
+            for (uint32_t i = s; i < e && !found; i += BFS_PULL_UNROLL) {
+                uint32_t p[BFS_PULL_UNROLL];
 #pragma unroll
-            for (int k = 0; k < BFS_PULL_UNROLL; k++) p[k] = i + k < e ? __ldg(a.rev_e + i + k) : 0u;
+                for (int k = 0; k < BFS_PULL_UNROLL; k++) p[k] = i + k < e ? __ldg(a.rev_e + i + k) : 0u;
 #pragma unroll
-            for (int k = 0; k < BFS_PULL_UNROLL; k++) found |= i + k < e && lv[p[k]] == depth;
+                for (int k = 0; k < BFS_PULL_UNROLL; k++) found |= i + k < e && lv[p[k]] == depth;
+            }
+            if (found) {
+                lv[v] = nd;
+                cnt.hit(&slot->frontier);
+                side.visit(a, nullptr, slot, static_cast<uint32_t>(v));   // statistics; the queue below
+            }
         }
-        if (found) {
-            lv[v] = nd;
-            cnt.hit(&slot->frontier);
-            side.visit(a, qnext, slot, static_cast<uint32_t>(v));
-        }
+        if constexpr (SIDE) if (qnext) wq.add(found, static_cast<uint32_t>(v), qnext, &slot->qlen);
     }
+    if constexpr (SIDE) if (qnext) wq.flush(qnext, &slot->qlen);
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -483,7 +492,7 @@ __global__ void __launch_bounds__(512) k_bfs_vwarp(BfsArgs a)
         }
     }
     cnt.finish(&slot->frontier);
-    side.finish(slot);
+    side.finish_block(slot);
 }
 
 // ---------------------------------------------------------------------------
