@@ -139,6 +139,10 @@ SIGNATURES = {
                                   C.c_uint32, C.c_void_p, C.POINTER(C.c_float), C.c_void_p]),
     "bw_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
                                  C.c_void_p]),
+    "bw_mlp_predict_host": (C.c_int, [C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float), C.c_uint32,
+                                      C.POINTER(C.c_float)]),
+    "bw_bfs_frontier_stats": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_uint32, C.c_int32,
+                                        C.POINTER(BfsLevelStats), C.c_void_p]),
     "bw_bfs_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
                                      C.c_void_p, C.c_int, C.c_uint32, C.POINTER(BfsResult),
                                      C.POINTER(BfsLevelStats), C.c_uint32, C.c_void_p]),

@@ -4,8 +4,10 @@ Compiles, in parallel, every translation unit of libbelewitte_gb300.so
 (hand-written CUDA for sm_103a plus the host C++ graph substrate) and links
 the shared library next to this file.  Used by ``__graft_entry__.build()``
 and by the package import when the library is missing.  Also builds the C++
-plugin libraries (``libbfskernel.so``, ``libpagerankkernel.so``) and the
-``kernel-runner`` driver from ``belewitte_gb300/plugin``.
+plugin libraries (``libbfskernel.so``, ``libpagerankkernel.so``), the
+``kernel-runner`` driver from ``belewitte_gb300/plugin`` and the shipped BFS
+predictor as a reference-format predictor library
+(``libbfs_mlp_predictor.so``).
 """
 from __future__ import annotations
 
@@ -116,6 +118,16 @@ def build_plugins(force: bool = False) -> list[Path]:
         out.append(target)
     with _cf.ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(_run, steps))
+    # the shipped learned predictor as a reference-format predictor library
+    # (kernel-runner -a bfs -k switch -m libbfs_mlp_predictor.so)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_bw_predictor_export", PKG / "predictor_export.py")
+    pe = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(pe)
+    if pe.DEFAULT_NPZ.exists():
+        if force or _stale(pe.DEFAULT_SO, [pe.DEFAULT_NPZ, Path(pe.__file__), LIB] + list(INCLUDE.glob("*.h"))):
+            pe.export_predictor()
+        out.append(pe.DEFAULT_SO)
     return out
 
 

@@ -452,6 +452,23 @@ struct Plan {
 };
 
 }  // namespace
+// The frontier {root} before level 0, with the statistics the level kernels
+// accumulate (the same formula as the side-statistics initialisation).
+__global__ void k_bfs_root_stats(const uint32_t *outdeg, uint32_t root, LevelSlot *out)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint32_t d = outdeg[root];
+        const float l = __log2f(1.0f + static_cast<float>(d));
+        *out = LevelSlot{};
+        out->frontier = 1;
+        out->qlen = 1;
+        out->fedges = d;
+        out->lsum = l;
+        out->lsq = l * l;
+        out->lmax_bits = __float_as_uint(l);
+    }
+}
+
 }  // namespace bw
 
 using namespace bw;
@@ -466,6 +483,41 @@ void bw_bfs_features(uint64_t fv, uint64_t fe, float lsum, float lsq, float lmax
     bwfeat::compute(static_cast<double>(fv), static_cast<double>(fe), lsum, lsq, lmax, static_cast<double>(n),
                     static_cast<double>(m), static_cast<double>(visited), static_cast<double>(edges_visited),
                     static_cast<double>(level), out);
+}
+
+int bw_mlp_predict_host(const float *params, uint32_t classes, const float *features, uint32_t n, float *probs)
+{
+    if (!params || !features || !probs || classes < 2 || classes > BW_MLP_MAX_CLASSES) return BW_ERR_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+        mlp_forward_host(params, classes, features + static_cast<size_t>(i) * F, probs + static_cast<size_t>(i) * classes);
+    return BW_OK;
+}
+
+int bw_bfs_frontier_stats(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32_t depth,
+                          bw_bfs_level_stats *out, void *stream)
+{
+    if (!ctx || !g || !out) return BW_ERR_INVALID_ARGUMENT;
+    if (!g->fwd_vertices) return BW_ERR_MISSING_REPRESENTATION;
+    cudaStream_t s = as_stream(stream);
+    LevelSlot sl{};
+    if (depth < 0) {
+        if (root >= g->vertex_count) return BW_ERR_INVALID_ARGUMENT;
+        BW_TRY(ensure_outdeg(ctx, g, s));
+        LevelSlot *d = nullptr;
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&d), sizeof(LevelSlot), s));
+        k_bfs_root_stats<<<1, 32, 0, s>>>(ctx->outdeg, root, d);
+        const cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) cudaMemcpyAsync(&sl, d, sizeof(LevelSlot), cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(d, s);
+        BW_CUDA(e);
+    } else {
+        // bw_bfs_level at this depth left its counts in slot depth % 3
+        if (!ctx->bfs_ctl) return BW_ERR_INVALID_ARGUMENT;
+        BW_CUDA(cudaMemcpyAsync(&sl, &ctx->bfs_ctl->slot[depth % 3], sizeof(LevelSlot), cudaMemcpyDeviceToHost, s));
+    }
+    BW_CUDA(cudaStreamSynchronize(s));
+    slot_stats(sl, -1, out);
+    return BW_OK;
 }
 
 int bw_mlp_init(float *params, uint32_t classes, const float *mu, const float *sd, uint64_t seed, void *stream)

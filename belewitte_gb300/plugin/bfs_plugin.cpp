@@ -101,6 +101,9 @@ class BfsImplementation : public ImplementationBase {
 };
 
 // `switch`: per-level variant choice by a predictor .so (bfs/bfs.cpp:83-106).
+// Beside the reference's four step properties (setProps, bfs/bfs.cpp:43-49)
+// it publishes the frontier's out-edge volume and log-degree moments, the
+// out-edges already visited and the depth, which the learned predictor reads.
 class BfsSwitch : public ImplementationBase, public SwitchBase {
   public:
     BfsSwitch() : SwitchBase(options, true)
@@ -110,6 +113,12 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
         rel_frontier_ = &add_algo_prop("frontier rel");
         abs_visited_ = &add_algo_prop("visited abs");
         rel_visited_ = &add_algo_prop("visited rel");
+        frontier_edges_ = &add_algo_prop("frontier edges");
+        log_sum_ = &add_algo_prop("frontier log degree sum");
+        log_sq_sum_ = &add_algo_prop("frontier log degree square sum");
+        log_max_ = &add_algo_prop("frontier log degree max");
+        visited_edges_ = &add_algo_prop("visited edges");
+        depth_ = &add_algo_prop("depth");
     }
 
   protected:
@@ -142,6 +151,9 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
             *rel_frontier_ = 1.0 / static_cast<double>(n);
             *abs_visited_ = 0;
             *rel_visited_ = 0;
+            *visited_edges_ = 0;
+            *depth_ = 0;
+            set_frontier_stats(-1);
             int variant = predict_initial();
             uint32_t frontier = 1;
             int32_t depth = 0;
@@ -159,6 +171,9 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
                     *rel_visited_ = abs_visited_->get() / static_cast<double>(n);
                     *abs_frontier_ = frontier;
                     *rel_frontier_ = abs_frontier_->get() / static_cast<double>(n);
+                    *visited_edges_ = visited_edges_->get() + frontier_edges_->get();
+                    *depth_ = depth;
+                    set_frontier_stats(depth - 1);
                     int next = predict();
                     if (next >= 0) variant = next;
                 }
@@ -168,8 +183,21 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
         run_.write(out);
     }
 
+    // Statistics of the frontier the level at `depth` found (-1: {root}).
+    void set_frontier_stats(int32_t depth)
+    {
+        bw_bfs_level_stats st{};
+        check_bw(bw_bfs_frontier_stats(shared_context(), &run_.graph.view, run_.root, depth, &st, nullptr),
+                 "frontier statistics");
+        *frontier_edges_ = static_cast<double>(st.frontier_edges);
+        *log_sum_ = st.log_degree_sum;
+        *log_sq_sum_ = st.log_degree_sq_sum;
+        *log_max_ = st.log_degree_max;
+    }
+
     BfsRun run_;
     prop_ref *abs_frontier_, *rel_frontier_, *abs_visited_, *rel_visited_;
+    prop_ref *frontier_edges_, *log_sum_, *log_sq_sum_, *log_max_, *visited_edges_, *depth_;
 };
 
 }  // namespace

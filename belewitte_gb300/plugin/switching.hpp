@@ -1,21 +1,26 @@
 // Predictor-driven variant switching of the plugin surface
 // (SwitchImplementation, ImplementationTemplate.hpp:545-908).
 //
-// A predictor is a shared library exporting, with C++ linkage as the
-// reference's exported decision trees do (benchmark-analysis
-// src/Predictor/Raw.hs:56-139):
+// A predictor is a shared library exporting, unmangled (extern "C") with
+// C++ types as the reference's exported decision trees do
+// (benchmark-analysis src/Predictor/Raw.hs:56-139):
 //   int32_t lookup();
 //   std::map<std::string, std::reference_wrapper<double>> propNames;
 //   std::vector<std::tuple<std::string,int64_t,size_t,size_t,size_t>> implNames;
 //   int32_t default_impl;
 // Properties named in propNames are re-pointed at the predictor's storage,
-// so setting them feeds lookup().  Without a model the switch runs
+// so setting them feeds lookup(); every other property gets storage of its
+// own (as the reference's setupLogging gives the logged ones,
+// ImplementationTemplate.hpp:845-867), so that it holds its value.  Without a model the switch runs
 // `edge-list` and only logs (ImplementationTemplate.hpp:709-720).
 // Log lines: graph:NAME:VALUE, step:N:NAME:VALUE, prediction:N:ID
 // (ImplementationTemplate.hpp:829-876).
 #pragma once
 
 #include <dlfcn.h>
+
+#include <map>
+#include <set>
 
 #include "framework.hpp"
 
@@ -65,6 +70,8 @@ class SwitchBase {
     {
         impls_.clear();
         ids_.clear();
+        bound_.clear();
+        storage_.clear();
         last_ = -1;
         step_ = 0;
         if (!model_.empty()) {
@@ -96,12 +103,16 @@ class SwitchBase {
                 ids_[idx] = std::get<1>(t);
             }
             if (missing) reportError("Missing properties/implementations!");
+            for (auto &p : props) bound_.insert(p.first);
         } else {
             lookup_ = nullptr;
             default_ = 0;
             impls_.push_back(lookup_variant(default_name));
             ids_.push_back(-1);
         }
+        for (auto *table : {&graph_props_, &algo_props_})
+            for (auto &p : *table)
+                if (!bound_.count(p.first)) *p.second = std::ref(storage_[p.first] = 0.0);
         if (!log_file_.empty()) {
             log_.open(log_file_);
             log_.imbue(std::locale("C"));
@@ -139,6 +150,8 @@ class SwitchBase {
         if (log_.is_open()) log_.close();
         for (auto &p : graph_props_) p.second->reset();
         for (auto &p : algo_props_) p.second->reset();
+        bound_.clear();
+        storage_.clear();
     }
 
   private:
@@ -170,5 +183,7 @@ class SwitchBase {
     size_t step_ = 0;
     std::vector<int> impls_;
     std::vector<int64_t> ids_;
+    std::set<std::string> bound_;              // properties the predictor owns
+    std::map<std::string, double> storage_;    // the others (map nodes do not move)
     std::ofstream log_;
 };

@@ -289,6 +289,20 @@ typedef struct bw_bfs_level_stats {
     float device_ms;              /* level time, when timing was requested */
 } bw_bfs_level_stats;
 
+/*
+ * The statistics of a frontier, for a host-side switch that picks the
+ * variant of each level (SwitchImplementation::predict,
+ * ImplementationTemplate.hpp:768-827, fed by setProps, bfs/bfs.cpp:43-49).
+ * depth < 0: the frontier {root} that level 0 expands (root's out-degree).
+ * depth >= 0: the vertices the bw_bfs_level call at `depth` newly visited,
+ * i.e. the frontier of level depth + 1; valid until three more levels run.
+ * Needs the forward CSR (the level kernels then accumulate the statistics).
+ * out->variant is 0xffffffff (not recorded) and out->device_ms 0.
+ */
+int bw_bfs_frontier_stats(bw_context *ctx, const bw_graph_view *g,
+                          uint32_t root, int32_t depth,
+                          bw_bfs_level_stats *out, void *stream);
+
 typedef struct bw_bfs_result {
     uint32_t level_count;         /* levels run (last one found nothing) */
     uint32_t reserved;
@@ -456,6 +470,12 @@ int bw_mlp_gradient(bw_context *ctx, const float *params, uint32_t classes,
 /* Softmax probabilities probs[n][K] (device). */
 int bw_mlp_predict(bw_context *ctx, const float *params, uint32_t classes,
                    const float *X, uint32_t n, float *probs, void *stream);
+
+/* The same forward pass on the host, with host params, X and probs, and the
+ * host loop's operation order (BW_LOOP_HOST below picks from it); a
+ * predictor library built from a trained model calls it. */
+int bw_mlp_predict_host(const float *params, uint32_t classes,
+                        const float *X, uint32_t n, float *probs);
 
 typedef struct bw_switch_config {
     const float *params;        /* device MLP parameters */
