@@ -438,6 +438,34 @@ int prepare(bw_context *ctx, const bw_graph_view *g, int reps, bool side, int32_
 
 }  // namespace
 
+// A graph without edges (the edge arrays may then be null): level 0 expands
+// {root} and finds nothing, so the root gets depth 0 and every other vertex
+// INT_MAX after one level (bfs/bfs.cpp:80-107); no level kernel runs.
+int bfs_edgeless(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t root, int32_t *levels,
+                 bw_bfs_result *result, bw_bfs_level_stats *stats, uint32_t stats_capacity, cudaStream_t s)
+{
+    if (!ctx || !levels) return BW_ERR_INVALID_ARGUMENT;
+    BW_TRY(validate_graph(g));
+    if (root >= g->vertex_count) return BW_ERR_INVALID_ARGUMENT;
+    if (!g->fwd_vertices && !g->rev_vertices) return BW_ERR_MISSING_REPRESENTATION;
+    BW_TRY(ensure_bfs_scratch(ctx, g->vertex_count, 0));
+    k_bfs_init_side<<<ctx->sm_count * 4, 256, 0, s>>>(levels, g->vertex_count, root, ctx->queue[0], ctx->bfs_ctl,
+                                                     0, nullptr);
+    BW_CUDA(cudaGetLastError());
+    BW_CUDA(cudaStreamSynchronize(s));
+    if (stats && stats_capacity) {
+        stats[0] = bw_bfs_level_stats{};
+        stats[0].variant = static_cast<uint32_t>(variant);
+    }
+    if (result) {
+        result->level_count = 1;
+        result->visited = 1;
+        result->traversed_edges = 0;
+        result->device_ms = 0.0;
+    }
+    return BW_OK;
+}
+
 // Shared with bw_learn.cu.
 int bfs_prepare(bw_context *ctx, const bw_graph_view *g, int reps, bool side, int32_t *levels, uint32_t root,
                 cudaStream_t s)
@@ -500,8 +528,16 @@ int bw_bfs_level(bw_context *ctx, const bw_graph_view *g, int variant, int32_t *
     if (!ctx || !levels || depth < 0) return BW_ERR_INVALID_ARGUMENT;
     BW_TRY(validate_graph(g));
     if (variant < 0 || variant >= VARIANT_COUNT) return BW_ERR_UNKNOWN_VARIANT;
-    BW_TRY(check_reps(g, variant_reps(variant)));
     if (!ctx->bfs_ctl || ctx->bfs_n_cap < g->vertex_count) return BW_ERR_INVALID_ARGUMENT;  // bw_bfs_init first
+    if (g->edge_count == 0) {
+        // no edges: the level visits nothing; its counts read as zero
+        cudaStream_t s = as_stream(stream);
+        BW_CUDA(cudaMemsetAsync(&ctx->bfs_ctl->slot[depth % 3], 0, sizeof(LevelSlot), s));
+        BW_CUDA(cudaStreamSynchronize(s));
+        if (frontier) *frontier = 0;
+        return BW_OK;
+    }
+    BW_TRY(check_reps(g, variant_reps(variant)));
     BW_TRY(ensure_bfs_scratch(ctx, g->vertex_count, g->edge_count));
     Launch plan;
     // Queue-driven variants need the queue kept by every level: levels run
@@ -531,6 +567,8 @@ int bw_bfs_run(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t ro
     const bool side = stats != nullptr && stats_capacity > 0;
     int reps = variant_reps(variant) | (side ? REP_FWD_CSR : 0);
     cudaStream_t s = as_stream(stream);
+    if (loop_mode != BW_LOOP_GRAPH && loop_mode != BW_LOOP_HOST) return BW_ERR_INVALID_ARGUMENT;
+    if (g && g->edge_count == 0) return bfs_edgeless(ctx, g, variant, root, levels, result, stats, stats_capacity, s);
     BW_TRY(prepare(ctx, g, reps, side, levels, root, s));
     if (loop_mode == BW_LOOP_GRAPH)
         return run_graph(ctx, g, variant, root, levels, cfg, max_levels, side, result, stats, stats_capacity, s);
@@ -555,6 +593,8 @@ int bw_bfs_run_schedule(bw_context *ctx, const bw_graph_view *g, const int32_t *
         reps |= variant_reps(schedule[i]);
     }
     cudaStream_t s = as_stream(stream);
+    if (g && g->edge_count == 0)
+        return bfs_edgeless(ctx, g, schedule[0], root, levels, result, stats, stats_capacity, s);
     BW_TRY(prepare(ctx, g, reps, true, levels, root, s));
     return run_host(ctx, g, schedule, schedule_len, root, levels, cfg, max_levels, time_levels, true,
                     result, stats, stats_capacity, s);

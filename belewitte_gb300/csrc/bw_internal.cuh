@@ -131,6 +131,8 @@ namespace bw {
 
 int ensure_bfs_scratch(bw_context *ctx, uint64_t n, uint64_t m);
 int ensure_outdeg(bw_context *ctx, const bw_graph_view *g, cudaStream_t s);
+int bfs_edgeless(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t root, int32_t *levels,
+                 bw_bfs_result *result, bw_bfs_level_stats *stats, uint32_t stats_capacity, cudaStream_t s);
 int ensure_pr_scratch(bw_context *ctx, uint64_t n, uint32_t iterations);
 int ensure_level_events(bw_context *ctx, uint32_t count);
 

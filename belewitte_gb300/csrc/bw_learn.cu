@@ -684,6 +684,9 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
     const uint32_t K = sw->classes;
     if (sw->fallback < 0 || static_cast<uint32_t>(sw->fallback) >= K) return BW_ERR_INVALID_ARGUMENT;
     cudaStream_t s = as_stream(stream);
+    if (loop_mode != BW_LOOP_GRAPH && loop_mode != BW_LOOP_HOST) return BW_ERR_INVALID_ARGUMENT;
+    if (g && g->edge_count == 0)      // no level kernel runs: nothing to choose
+        return bfs_edgeless(ctx, g, sw->candidates[sw->fallback], root, levels, result, stats, stats_cap, s);
     int reps = 1;
     for (uint32_t k = 0; k < K; k++) {
         if (bfs_variant_reps(sw->candidates[k]) == 0) return BW_ERR_UNKNOWN_VARIANT;

@@ -64,7 +64,7 @@ using namespace bw;
 extern "C" int bw_bfs_run_noalloc(const bw_graph_view *g, uint32_t root, int32_t *levels, uint32_t max_levels,
                                   uint32_t *level_count, void *stream)
 {
-    if (!g || !levels || !g->fwd_vertices || !g->fwd_edges) return BW_ERR_INVALID_ARGUMENT;
+    if (!g || !levels || !g->fwd_vertices || (g->edge_count && !g->fwd_edges)) return BW_ERR_INVALID_ARGUMENT;
     if (g->vertex_count == 0 || root >= g->vertex_count) return BW_ERR_INVALID_ARGUMENT;
     if (g->vertex_count > NOALLOC_MAX_VERTICES || g->edge_count > NOALLOC_MAX_EDGES) return BW_ERR_TOO_LARGE;
     NoAllocScratch *sc = nullptr;
@@ -95,6 +95,11 @@ extern "C" int bw_bfs_run_noalloc(const bw_graph_view *g, uint32_t root, int32_t
     // sets the first queue to {root}; the queues need no clearing.
     k_bfs_init_side<<<sm * 4, 256, 0, s>>>(levels, n, root, sc->q0, &sc->ctl, max_levels, nullptr);
     BW_CUDA(cudaGetLastError());
+    if (g->edge_count == 0) {          // level 0 finds nothing (the edge array may be null)
+        BW_CUDA(cudaStreamSynchronize(s));
+        if (level_count) *level_count = 1;
+        return BW_OK;
+    }
     uint32_t level = 0;
     for (;;) {
         if (level >= max_levels) {

@@ -19,6 +19,7 @@
 // segmented reductions sum in another order (the reference's own float
 // atomics make its order arbitrary too).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <cooperative_groups.h>
 #include <cub/cub.cuh>
@@ -1454,6 +1455,13 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr
     }
 }
 
+// Every rank set to one value (graphs without edges).
+__global__ void k_pr_fill(float *__restrict__ ranks, uint64_t n, float value)
+{
+    for (uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; v < n; v += uint64_t(gridDim.x) * blockDim.x)
+        ranks[v] = value;
+}
+
 }  // namespace
 }  // namespace bw
 
@@ -1786,6 +1794,42 @@ void free_relabel(Relabel &r, cudaStream_t s)
 }
 
 // Runs a (possibly switching) schedule of variants of one semantics class.
+// A graph without edges (its edge arrays may be null): every in-sum is +0
+// and every out-degree 0, so every iteration gives each vertex the same
+// rank, consolidateRank's (float)((1 - d) / N + (double)(d * 0))
+// (pagerank/pagerank.cu:125-140) or consolidateRankNoDiv's
+// (1 - d) / (float)N + d * 0 (pagerank/pagerank.cu:142-165), and the
+// first iteration's diff is N |rank - 1/N|.  Computed on the host in IEEE
+// single and double arithmetic, bit-identical to the device's
+// consolidation; one fill kernel writes the ranks.
+int run_edgeless(bw_context *ctx, uint64_t n, bool nodiv, uint32_t iterations, float *ranks, int time_iterations,
+                 float *iteration_ms, bw_pagerank_result *result, float *diffs_host, cudaStream_t s)
+{
+    const float init = 1.0f / static_cast<float>(n);
+    const float value = iterations == 0 ? init
+                        : nodiv ? (1.0f - DAMPING) / static_cast<float>(n)
+                                : static_cast<float>((1.0 - static_cast<double>(DAMPING)) / static_cast<double>(n));
+    BW_CUDA(cudaEventRecord(ctx->ev_start, s));
+    k_pr_fill<<<ctx->sm_count * 4, 256, 0, s>>>(ranks, n, value);
+    BW_CUDA(cudaGetLastError());
+    BW_CUDA(cudaEventRecord(ctx->ev_stop, s));
+    BW_CUDA(cudaEventSynchronize(ctx->ev_stop));
+    const float first = static_cast<float>(static_cast<double>(n) * std::fabs(static_cast<double>(value) - init));
+    if (diffs_host)
+        for (uint32_t j = 0; j < iterations; j++) diffs_host[j] = j == 0 ? first : 0.0f;
+    if (time_iterations && iteration_ms)
+        for (uint32_t j = 0; j < iterations; j++) iteration_ms[j] = 0.0f;
+    if (result) {
+        float ms = 0.0f;
+        BW_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+        result->iterations = iterations;
+        result->kernel_launches = 1;
+        result->last_diff = iterations == 0 ? 0.0f : iterations == 1 ? first : 0.0f;
+        result->device_ms = ms;
+    }
+    return BW_OK;
+}
+
 int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
                  uint32_t schedule_len, uint32_t iterations, float *ranks,
                  const bw_launch_config *cfg, int loop_mode, int time_iterations,
@@ -1812,6 +1856,11 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
             v == PR_VERTEX_PULL_WARP_NODIV)
             need_heavy = true;
         if (uses_rowlen(v)) any_rowlen = true; else any_deg = true;
+    }
+    if (g->edge_count == 0) {
+        if (!g->fwd_vertices && !g->rev_vertices) return BW_ERR_MISSING_REPRESENTATION;
+        return run_edgeless(ctx, g->vertex_count, nodiv, iterations, ranks, time_iterations, iteration_ms, result,
+                            diffs_host, as_stream(stream));
     }
     BW_TRY(check_reps(g, reps));
     if (any_rowlen && any_deg && !g->fwd_vertices) return BW_ERR_MISSING_REPRESENTATION;

@@ -69,6 +69,12 @@ const char *bw_version(void);
  *   StructEdgeList: {in,out} pairs, fwd_struct_edges[2M] / rev_struct_edges[2M]
  *
  * For a symmetric graph the forward and reverse arrays may alias.
+ *
+ * A graph without edges (edge_count 0) needs only fwd_vertices or
+ * rev_vertices; its edge arrays may be NULL.  Every BFS entry point then
+ * gives the root depth 0 and every other vertex INT_MAX after one level,
+ * and PageRank gives every vertex the constant rank of a zero in-sum, with
+ * no level or iteration kernel run.
  */
 typedef struct bw_graph_view {
     uint64_t vertex_count;
