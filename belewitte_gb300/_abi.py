@@ -74,7 +74,7 @@ class MlpTrainConfig(C.Structure):
 
 class SwitchConfig(C.Structure):
     _fields_ = [("params", C.c_void_p), ("classes", C.c_uint32), ("fallback", C.c_int32),
-                ("candidates", C.POINTER(C.c_int32)), ("threshold", C.c_float), ("reserved", C.c_uint32)]
+                ("candidates", C.POINTER(C.c_int32)), ("threshold", C.c_float), ("flags", C.c_uint32)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/belewitte_gb300.h

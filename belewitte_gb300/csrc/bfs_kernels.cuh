@@ -174,6 +174,13 @@ struct WarpQueue {
     }
 };
 
+// Hint that the 128-byte line holding p will be read soon (L2 only).
+// Callers pass addresses inside their arrays.
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Relax v to nd; true for exactly one caller per newly visited vertex.
 // The plain pre-check only filters: a stale read can only be INF or nd.
 __device__ __forceinline__ bool relax(int32_t *levels, uint32_t v, int32_t nd)
@@ -694,8 +701,9 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
 //  * each block holds a share of the frontier in shared memory as
 //    {vertex, row start, row end}: a level reads no queue and no offsets
 //    from global memory;
-//  * a neighbour is claimed with one atomicMin on its depth; the winner
-//    loads the neighbour's row bounds into its block's next list;
+//  * a neighbour is claimed with one atomicMin on its depth, issued with
+//    its row bounds' loads and the lane's other claims; the winner puts the
+//    bounds in its block's next list;
 //  * after the level's one cluster barrier, every block reads the blocks'
 //    counts and then its equal share of the next frontier from the other
 //    blocks' shared memory (a wavefront found by one block would otherwise
@@ -711,9 +719,6 @@ __global__ void __launch_bounds__(256) k_bfs_frontier_pull(BfsArgs a)
 // iteration return at once, and leaves that level's bookkeeping to the step
 // kernel.  The leader does the bookkeeping of the levels it completes.
 // ---------------------------------------------------------------------------
-constexpr uint32_t CLUSTER_LIST = 4096;            // frontier entries per block list
-constexpr uint32_t CLUSTER_CAP = CLUSTER_LIST * CLUSTER_CTAS;   // frontier vertices
-constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;        // frontier out-edges
 constexpr uint32_t CLUSTER_HEAVY = 1024;           // rows above: the full-GPU kernels
 constexpr int CLUSTER_UNROLL = 4;
 static_assert(CLUSTER_THREADS == 32 * 32, "the block's counts are reduced by one warp, one lane per warp");
@@ -801,9 +806,15 @@ k_bfs_cluster(BfsArgs a)
         uint32_t hits = 0, heavy = 0;
         unsigned long long fe = 0;
         float ls = 0.f, lq = 0.f, lm = 0.f;
-        auto claim = [&](uint32_t u) {
-            if (atomicMin(&lv[u], nd) <= nd) return;
-            const uint32_t us = a.fwd_v[u], ue = a.fwd_v[u + 1];
+        // a claimed neighbour u with row [us, ue): its counts and its entry
+        auto claim = [&](uint32_t u, uint32_t us, uint32_t ue) {
+            // Next-line prefetch: where vertex ids follow the graph's
+            // geometry (grids, meshes, road networks) the wavefront reaches
+            // u's id neighbours within a few levels, and the first touch of
+            // their lines would put an HBM miss on the level's critical path.
+            if (ue + 32 < a.m) prefetch_l2(a.fwd_e + ue + 32);
+            if (u + 33 <= a.n) prefetch_l2(a.fwd_v + u + 33);
+            if (u + 32 < a.n) prefetch_l2(lv + u + 32);
             hits++;
             fe += ue - us;
             heavy += ue - us > CLUSTER_HEAVY ? 1u : 0u;
@@ -849,9 +860,26 @@ k_bfs_cluster(BfsArgs a)
                         u[jj] = __ldg(a.fwd_e + s_start[wib][seg] + (k - s_excl[wib][seg]));
                     }
                 }
+                // A level is a chain of dependent accesses, so every lane's
+                // neighbours go out together: their row bounds (loaded
+                // whether or not the claim wins) and their atomics are all
+                // in flight before any result is used.
+                uint32_t us[CLUSTER_UNROLL], ue[CLUSTER_UNROLL];
+                int32_t old[CLUSTER_UNROLL];
+#pragma unroll
+                for (int jj = 0; jj < CLUSTER_UNROLL; jj++) {
+                    us[jj] = ue[jj] = 0;
+                    if (u[jj] != 0xffffffffu) {
+                        us[jj] = __ldg(a.fwd_v + u[jj]);
+                        ue[jj] = __ldg(a.fwd_v + u[jj] + 1);
+                    }
+                }
 #pragma unroll
                 for (int jj = 0; jj < CLUSTER_UNROLL; jj++)
-                    if (u[jj] != 0xffffffffu) claim(u[jj]);
+                    old[jj] = u[jj] != 0xffffffffu ? atomicMin(&lv[u[jj]], nd) : nd;
+#pragma unroll
+                for (int jj = 0; jj < CLUSTER_UNROLL; jj++)
+                    if (old[jj] > nd) claim(u[jj], us[jj], ue[jj]);
             }
             __syncwarp();
         }

@@ -162,6 +162,9 @@ size_t bfs_cluster_smem();                    // its dynamic shared memory
 int bfs_cluster_prepare();                    // allows that much on the current device
 constexpr unsigned CLUSTER_CTAS = 8;
 constexpr unsigned CLUSTER_THREADS = 1024;
+constexpr uint32_t CLUSTER_LIST = 4096;            // frontier entries per block list
+constexpr uint32_t CLUSTER_CAP = CLUSTER_LIST * CLUSTER_CTAS;   // frontier vertices the cluster kernel takes
+constexpr unsigned long long CLUSTER_EDGE_CAP = 65536;        // and their out-edges
 
 // Reference Backend::computeDivision (Backend.cpp:52-70).
 void compute_division(uint64_t count, uint32_t sm, uint32_t max_tpb,

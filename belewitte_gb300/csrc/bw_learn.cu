@@ -341,6 +341,7 @@ struct PredictArgs {
     float threshold;
     uint64_t n, m;
     cudaGraphConditionalHandle sw;
+    int32_t cluster_k;          // frontier-push's candidate index for cluster-sized frontiers, or -1
 };
 
 // Runs before every level inside the device loop: features of the current
@@ -359,6 +360,18 @@ __global__ void __launch_bounds__(PREDICT_THREADS) k_bfs_predict(PredictArgs a)
     for (uint32_t i = tid; i < P; i += PREDICT_THREADS) sp[i] = a.params[i];
     BfsCtl *c = a.ctl;
     const int32_t L = c->depth;
+    if (a.cluster_k >= 0) {
+        // a frontier the cluster kernel takes goes to frontier-push (the
+        // decision is uniform: every thread reads the same slot)
+        const LevelSlot s = c->slot[(L + 2) % 3];
+        if (s.qlen > 0 && s.qlen <= CLUSTER_CAP && s.fedges <= CLUSTER_EDGE_CAP) {
+            if (tid == 0) {
+                c->variant = a.cluster_k;
+                cudaGraphSetConditional(a.sw, static_cast<unsigned>(a.cluster_k));
+            }
+            return;
+        }
+    }
     if (tid == 0) {
         const LevelSlot s = c->slot[(L + 2) % 3];
         float lmax;
@@ -781,7 +794,11 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             fail(e, "handle(switch)"); break;
         }
         // predict kernel node
-        PredictArgs pa{ctx->bfs_ctl, sw->params, K, sw->fallback, sw->threshold, n, m, swh};
+        int32_t cluster_k = -1;
+        if (!(sw->flags & BW_SWITCH_MLP_ONLY))
+            for (uint32_t k = 0; k < K; k++)
+                if (sw->candidates[k] == 32) cluster_k = static_cast<int32_t>(k);   // frontier-push
+        PredictArgs pa{ctx->bfs_ctl, sw->params, K, sw->fallback, sw->threshold, n, m, swh, cluster_k};
         cudaKernelNodeParams kp = {};
         void *pargs[] = {&pa};
         kp.func = reinterpret_cast<void *>(k_bfs_predict);

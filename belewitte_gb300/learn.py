@@ -270,10 +270,12 @@ class Predictor:
     fallback: int
     threshold: float
 
-    def switch_config(self):
+    def switch_config(self, mlp_only: bool = False):
+        """bw_switch_config; mlp_only sets BW_SWITCH_MLP_ONLY (the device
+        loop then leaves cluster-sized frontiers to the MLP too)."""
         ids = (C.c_int32 * len(self.candidates))(*[bfs_variant_id(c) for c in self.candidates])
         cfg = _abi.SwitchConfig(C.c_void_p(self.params.data_ptr()), len(self.candidates), self.fallback, ids,
-                                self.threshold, 0)
+                                self.threshold, 1 if mlp_only else 0)
         cfg._keep = ids
         return cfg
 
@@ -293,13 +295,13 @@ def load_predictor(path=PREDICTOR_PATH, device: int = 0) -> Predictor:
 
 
 def run_learned(ctx, g, predictor: Predictor, root: int, *, loop: str = "graph", levels=None, stats: bool = True,
-                max_levels: int = 0):
+                max_levels: int = 0, mlp_only: bool = False):
     """BFS with the learned per-level switch (bw_bfs_run_learned)."""
     import torch
     from . import BfsRun, _stats_list
     if levels is None:
         levels = torch.empty(g.vertex_count, dtype=torch.int32, device=g.device)
-    cfg = predictor.switch_config()
+    cfg = predictor.switch_config(mlp_only)
     res = _abi.BfsResult()
     cap = min(max_levels or g.vertex_count + 1, 1 << 16) if stats else 0
     arr = (_abi.BfsLevelStats * cap)() if cap else None

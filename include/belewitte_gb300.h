@@ -489,8 +489,16 @@ typedef struct bw_switch_config {
     int32_t fallback;           /* index into candidates */
     const int32_t *candidates;  /* host array of K BFS variant ids */
     float threshold;            /* below this top probability use fallback */
-    uint32_t reserved;
+    uint32_t flags;             /* BW_SWITCH_* */
 } bw_switch_config;
+
+/* BW_LOOP_GRAPH normally runs a level whose frontier frontier-push's
+ * cluster kernel can take (at most 32,768 vertices and 65,536 out-edges)
+ * with frontier-push when it is a candidate: that kernel then carries on
+ * through the following small levels on chip, one cluster barrier per
+ * level, which no per-level choice can match on high-diameter graphs.
+ * BW_SWITCH_MLP_ONLY leaves every level to the MLP, as BW_LOOP_HOST does. */
+enum { BW_SWITCH_MLP_ONLY = 1 };
 
 /*
  * BFS whose every level runs the variant the MLP picks from that level's

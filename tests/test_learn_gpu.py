@@ -124,6 +124,28 @@ def test_device_and_host_predictions_agree(ctx):
     h = catalog()["rmat14"][0]()
     g = bw.DeviceGraph(h)
     r = h.max_out_degree_vertex()
-    a = learn.run_learned(ctx, g, pred, r, loop="graph")
+    a = learn.run_learned(ctx, g, pred, r, loop="graph", mlp_only=True)
     b = learn.run_learned(ctx, g, pred, r, loop="host")
     assert [s["variant"] for s in a.level_stats] == [s["variant"] for s in b.level_stats]
+
+
+def test_cluster_sized_frontiers_run_frontier_push(ctx):
+    """The device loop gives every level whose frontier the cluster kernel
+    takes to frontier-push, and the MLP the rest; depths are unchanged."""
+    pred = learn.load_predictor()
+    fp = bw.bfs_variant_id("frontier-push")
+    for name in ["grid", "rmat14", "chain"]:
+        make, root = catalog()[name]
+        h = make()
+        g = bw.DeviceGraph(h)
+        r = root_of(h, root)
+        lv, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, r)
+        run = learn.run_learned(ctx, g, pred, r, loop="graph")
+        assert np.array_equal(run.levels.cpu().numpy(), lv), name
+        deg = np.diff(h.fwd_vertices.astype(np.int64))
+        frontier, fedges = 1, int(deg[r])
+        for L, s in enumerate(run.level_stats):
+            if frontier <= 32768 and fedges <= 65536:
+                assert s["variant"] == fp, (name, L)
+            frontier = int((lv == L + 1).sum())
+            fedges = int(deg[lv == L + 1].sum())
