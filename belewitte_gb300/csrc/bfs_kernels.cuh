@@ -739,8 +739,6 @@ __global__ void __cluster_dims__(CLUSTER_CTAS, 1, 1) __launch_bounds__(CLUSTER_T
 k_bfs_cluster(BfsArgs a)
 {
     extern __shared__ uint32_t cl_lists[];
-    __shared__ uint32_t s_excl[CLUSTER_THREADS / 32][32];
-    __shared__ uint32_t s_start[CLUSTER_THREADS / 32][32];
     __shared__ ClusterCounts s_cnt[2];             // by level parity; read by the other blocks
     __shared__ ClusterCounts s_tot;                // the cluster's totals
     __shared__ uint32_t s_pre[CLUSTER_CTAS + 1];    // exclusive prefix of the blocks' next lists
@@ -806,8 +804,8 @@ k_bfs_cluster(BfsArgs a)
         uint32_t hits = 0, heavy = 0;
         unsigned long long fe = 0;
         float ls = 0.f, lq = 0.f, lm = 0.f;
-        // a claimed neighbour u with row [us, ue): its counts and its entry
-        auto claim = [&](uint32_t u, uint32_t us, uint32_t ue) {
+        // a claimed neighbour u with row [us, ue): its counts and its entry k
+        auto claim = [&](uint32_t u, uint32_t us, uint32_t ue, uint32_t k) {
             // Next-line prefetch: where vertex ids follow the graph's
             // geometry (grids, meshes, road networks) the wavefront reaches
             // u's id neighbours within a few levels, and the first touch of
@@ -822,7 +820,6 @@ k_bfs_cluster(BfsArgs a)
                 const float l = __log2f(1.0f + static_cast<float>(ue - us));
                 ls += l; lq += l * l; lm = fmaxf(lm, l);
             }
-            const uint32_t k = atomicAdd(&s_n, 1u);
             if (k < CLUSTER_LIST) {
                 nv[k] = u;
                 ns[k] = us;
@@ -844,21 +841,21 @@ k_bfs_cluster(BfsArgs a)
                 const uint32_t y = __shfl_up_sync(FULL_MASK, incl, o);
                 if (lane >= static_cast<unsigned>(o)) incl += y;
             }
-            const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
-            s_excl[wib][lane] = incl - d;
-            s_start[wib][lane] = s;
-            __syncwarp();
-            uint32_t seg = 0;
+            const uint32_t total = __shfl_sync(FULL_MASK, incl, 31), excl = incl - d;
             for (uint32_t k0 = 0; k0 < total; k0 += 32 * CLUSTER_UNROLL) {
                 uint32_t u[CLUSTER_UNROLL];
 #pragma unroll
                 for (int jj = 0; jj < CLUSTER_UNROLL; jj++) {
+                    // edge k of the concatenated rows belongs to the last
+                    // lane whose exclusive prefix is <= k (that lane's row
+                    // is not empty): a binary search over the lanes
                     const uint32_t k = k0 + jj * 32 + lane;
-                    u[jj] = 0xffffffffu;
-                    if (k < total) {
-                        while (seg < 31 && s_excl[wib][seg + 1] <= k) seg++;
-                        u[jj] = __ldg(a.fwd_e + s_start[wib][seg] + (k - s_excl[wib][seg]));
-                    }
+                    uint32_t seg = 0;
+#pragma unroll
+                    for (uint32_t b = 16; b > 0; b >>= 1)
+                        if (__shfl_sync(FULL_MASK, excl, seg + b) <= k) seg += b;
+                    const uint32_t rs = __shfl_sync(FULL_MASK, s, seg), ex = __shfl_sync(FULL_MASK, excl, seg);
+                    u[jj] = k < total ? __ldg(a.fwd_e + rs + (k - ex)) : 0xffffffffu;
                 }
                 // A level is a chain of dependent accesses, so every lane's
                 // neighbours go out together: their row bounds (loaded
@@ -877,11 +874,18 @@ k_bfs_cluster(BfsArgs a)
 #pragma unroll
                 for (int jj = 0; jj < CLUSTER_UNROLL; jj++)
                     old[jj] = u[jj] != 0xffffffffu ? atomicMin(&lv[u[jj]], nd) : nd;
+                // the winners' entries: one shared atomic per warp and step
 #pragma unroll
-                for (int jj = 0; jj < CLUSTER_UNROLL; jj++)
-                    if (old[jj] > nd) claim(u[jj], us[jj], ue[jj]);
+                for (int jj = 0; jj < CLUSTER_UNROLL; jj++) {
+                    const bool win = old[jj] > nd;
+                    const unsigned wm = __ballot_sync(FULL_MASK, win);
+                    if (wm == 0) continue;
+                    uint32_t base = 0;
+                    if (lane == 0) base = atomicAdd(&s_n, static_cast<uint32_t>(__popc(wm)));
+                    base = __shfl_sync(FULL_MASK, base, 0);
+                    if (win) claim(u[jj], us[jj], ue[jj], base + __popc(wm & ((1u << lane) - 1u)));
+                }
             }
-            __syncwarp();
         }
         // the block's counts
         for (int o = 16; o > 0; o >>= 1) {
