@@ -372,7 +372,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
                 a.skip_check = 1;
                 a.log = log;
                 a.log_cap = log_cap;
-                bfs_cluster_kernel(side)<<<CLUSTER_CTAS, CLUSTER_THREADS, bfs_cluster_smem(), cap>>>(a);
+                bfs_cluster_kernel(side ? 1 : 0)<<<CLUSTER_CTAS, CLUSTER_THREADS, bfs_cluster_smem(), cap>>>(a);
             }
             plan.k<<<plan.grid, plan.block, plan.smem, cap>>>(a);
             if (plan.k2) plan.k2<<<hub_grid(plan.grid, plan.block), 256, 0, cap>>>(a);

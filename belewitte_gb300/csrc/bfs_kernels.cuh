@@ -730,11 +730,14 @@ struct ClusterCounts {
     uint32_t frontier;            // new vertices of the level found by this block
     uint32_t listed;              // of those, in the block's next list
     unsigned long long fedges;    // their out-edges
-    float ls, lq, lm;             // log-degree statistics (SIDE)
+    float ls, lq, lm;             // log-degree statistics (STATS == 1)
     uint32_t heavy;               // of those, rows above CLUSTER_HEAVY
 };
 
-template<bool SIDE>
+// STATS: 0 none; 1 the log-degree statistics of every level (accumulated
+// per claim, for a level log); 2 only those of a level handed over (what
+// the next level's choice reads), computed from its frontier at handover.
+template<int STATS>
 __global__ void __cluster_dims__(CLUSTER_CTAS, 1, 1) __launch_bounds__(CLUSTER_THREADS)
 k_bfs_cluster(BfsArgs a)
 {
@@ -746,6 +749,7 @@ k_bfs_cluster(BfsArgs a)
     __shared__ uint32_t r_hits[CLUSTER_THREADS / 32], r_heavy[CLUSTER_THREADS / 32];
     __shared__ float r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32], r_lm[CLUSTER_THREADS / 32];
     __shared__ uint32_t s_n, s_cur_n;
+    __shared__ float s_hand[3];                    // this block's part of a handed-over frontier's statistics
     cg::cluster_group cl = cg::this_cluster();
     BfsCtl *ctl = a.ctl;
     const unsigned rank = cl.block_rank(), tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
@@ -816,7 +820,7 @@ k_bfs_cluster(BfsArgs a)
             hits++;
             fe += ue - us;
             heavy += ue - us > CLUSTER_HEAVY ? 1u : 0u;
-            if constexpr (SIDE) {
+            if constexpr (STATS == 1) {
                 const float l = __log2f(1.0f + static_cast<float>(ue - us));
                 ls += l; lq += l * l; lm = fmaxf(lm, l);
             }
@@ -892,7 +896,7 @@ k_bfs_cluster(BfsArgs a)
             hits += __shfl_xor_sync(FULL_MASK, hits, o);
             heavy += __shfl_xor_sync(FULL_MASK, heavy, o);
             fe += __shfl_xor_sync(FULL_MASK, fe, o);
-            if constexpr (SIDE) {
+            if constexpr (STATS == 1) {
                 ls += __shfl_xor_sync(FULL_MASK, ls, o);
                 lq += __shfl_xor_sync(FULL_MASK, lq, o);
                 lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
@@ -950,17 +954,60 @@ k_bfs_cluster(BfsArgs a)
             // then the blocks' lists) and the level's slot
             const uint32_t at = (f - listed_all) + s_pre[rank], mine = s_cnt[p].listed;
             for (uint32_t i = tid; i < mine; i += CLUSTER_THREADS) qnext[at + i] = nv[i];
+            float hls = ls_all, hlq = lq_all, hlm = lm_all;
+            if constexpr (STATS == 2) {
+                // The handed-over frontier's log-degree statistics: this
+                // block's list entries and its slice of the overflow, which
+                // the other blocks wrote to the global queue before the
+                // counts' cluster barrier (read past L1).
+                float ls = 0.f, lq = 0.f, lm = 0.f;
+                auto add = [&](uint32_t deg) {
+                    const float l = __log2f(1.0f + static_cast<float>(deg));
+                    ls += l; lq += l * l; lm = fmaxf(lm, l);
+                };
+                for (uint32_t i = tid; i < mine; i += CLUSTER_THREADS) add(ne[i] - ns[i]);
+                const uint32_t ov = f - listed_all, per = (ov + CLUSTER_CTAS - 1) / CLUSTER_CTAS;
+                const uint32_t ob = min(ov, rank * per), oe = min(ov, ob + per);
+                for (uint32_t i = ob + tid; i < oe; i += CLUSTER_THREADS) {
+                    const uint32_t v = __ldcg(qnext + i);
+                    add(a.fwd_v[v + 1] - a.fwd_v[v]);
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                    lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                    lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+                }
+                if (lane == 0) { r_ls[wib] = ls; r_lq[wib] = lq; r_lm[wib] = lm; }
+                __syncthreads();
+                if (wib == 0) {
+                    ls = r_ls[lane]; lq = r_lq[lane]; lm = r_lm[lane];
+                    for (int o = 16; o > 0; o >>= 1) {
+                        ls += __shfl_xor_sync(FULL_MASK, ls, o);
+                        lq += __shfl_xor_sync(FULL_MASK, lq, o);
+                        lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+                    }
+                    if (lane == 0) { s_hand[0] = ls; s_hand[1] = lq; s_hand[2] = lm; }
+                }
+                cl.sync();                               // every block's part is out
+                if (leader) {
+                    hls = hlq = hlm = 0.f;
+                    for (unsigned q = 0; q < CLUSTER_CTAS; q++) {
+                        const float *h = cl.map_shared_rank(s_hand, q);
+                        hls += h[0]; hlq += h[1]; hlm = fmaxf(hlm, h[2]);
+                    }
+                }
+            }
             if (leader) {
                 slot->frontier = f;
                 slot->qlen = f;
                 slot->fedges = fe_all;
-                slot->lsum = ls_all;
-                slot->lsq = lq_all;
-                slot->lmax_bits = __float_as_uint(lm_all);
+                slot->lsum = hls;
+                slot->lsq = hlq;
+                slot->lmax_bits = __float_as_uint(hlm);
                 slot->heavy = 0;
                 ctl->skip = 1;
             }
-            cl.sync();                                   // no block leaves while others may read its counts
+            cl.sync();                                   // no block leaves while others may read its shared memory
             return;
         }
         if (leader) {                                      // the step kernel's bookkeeping for level L

@@ -32,17 +32,15 @@ BfsKernelFn bfs_frontier_push_kernel(bool side)
 BfsKernelFn bfs_hub_kernel(bool side)
 { return side ? k_bfs_hub_chunks<true> : k_bfs_hub_chunks<false>; }
 
-BfsKernelFn bfs_cluster_kernel(bool side)
-{ return side ? k_bfs_cluster<true> : k_bfs_cluster<false>; }
+BfsKernelFn bfs_cluster_kernel(int stats)
+{ return stats == 1 ? k_bfs_cluster<1> : stats == 2 ? k_bfs_cluster<2> : k_bfs_cluster<0>; }
 
 size_t bfs_cluster_smem() { return CLUSTER_SMEM; }
 
 int bfs_cluster_prepare()
 {
-    BW_CUDA(cudaFuncSetAttribute(k_bfs_cluster<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(CLUSTER_SMEM)));
-    BW_CUDA(cudaFuncSetAttribute(k_bfs_cluster<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(CLUSTER_SMEM)));
+    for (BfsKernelFn k : {k_bfs_cluster<0>, k_bfs_cluster<1>, k_bfs_cluster<2>})
+        BW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(CLUSTER_SMEM)));
     return BW_OK;
 }
 

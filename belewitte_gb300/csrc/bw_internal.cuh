@@ -157,7 +157,9 @@ BfsKernelFn bfs_hub_kernel(bool side);
 inline unsigned hub_grid(unsigned grid, unsigned block)
 { return static_cast<unsigned>((static_cast<unsigned long long>(grid) * block + 255) / 256); }
 BfsKernelFn bfs_frontier_pull_kernel(bool side);
-BfsKernelFn bfs_cluster_kernel(bool side);   // 8-CTA cluster, CLUSTER_CTAS blocks of 1024 threads
+// the 8-block cluster kernel (CLUSTER_CTAS blocks of 1024 threads); stats:
+// 0 none, 1 every level's, 2 only a handed-over level's
+BfsKernelFn bfs_cluster_kernel(int stats);
 size_t bfs_cluster_smem();                    // its dynamic shared memory
 int bfs_cluster_prepare();                    // allows that much on the current device
 constexpr unsigned CLUSTER_CTAS = 8;

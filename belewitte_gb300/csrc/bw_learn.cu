@@ -825,7 +825,9 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             cudaGraphNode_t first = nullptr;
             if (sw->candidates[k] == 32) {      // frontier-push: small-frontier cluster path first
                 cudaKernelNodeParams cp = {};
-                cp.func = reinterpret_cast<void *>(bfs_cluster_kernel(true));
+                // the level log needs every level's statistics; otherwise
+                // only a handed-over level's, which the next prediction reads
+                cp.func = reinterpret_cast<void *>(bfs_cluster_kernel(log_cap ? 1 : 2));
                 cp.gridDim = dim3(CLUSTER_CTAS);
                 cp.blockDim = dim3(CLUSTER_THREADS);
                 cp.sharedMemBytes = static_cast<unsigned>(bfs_cluster_smem());

@@ -149,3 +149,21 @@ def test_cluster_sized_frontiers_run_frontier_push(ctx):
                 assert s["variant"] == fp, (name, L)
             frontier = int((lv == L + 1).sum())
             fedges = int(deg[lv == L + 1].sum())
+
+
+def test_learned_graph_loop_without_level_log(ctx):
+    """Without a level log the device loop's cluster kernel computes the
+    statistics of a handed-over frontier at handover only; depths and the
+    level count stay exact, on graphs whose frontiers outgrow the cluster
+    kernel (R-MAT, BA) and on ones that stay in it (grid, chain)."""
+    pred = learn.load_predictor()
+    for name in ["rmat14", "rmat12_sym", "ba", "grid", "chain", "star"]:
+        make, root = catalog()[name]
+        h = make()
+        g = bw.DeviceGraph(h)
+        r = root_of(h, root)
+        lv, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, r)
+        for stats in (False, True):
+            run = learn.run_learned(ctx, g, pred, r, loop="graph", stats=stats)
+            assert np.array_equal(run.levels.cpu().numpy(), lv), (name, stats)
+            assert run.level_count == len(cnt), (name, stats)
