@@ -143,6 +143,11 @@ SIGNATURES = {
                                       C.POINTER(C.c_float)]),
     "bw_bfs_frontier_stats": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_uint32, C.c_int32,
                                         C.POINTER(BfsLevelStats), C.c_void_p]),
+    "bw_pagerank_features": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_uint32, C.POINTER(C.c_float),
+                                       C.c_void_p]),
+    "bw_pagerank_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
+                                          C.c_void_p, C.c_int, C.POINTER(PagerankResult), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_int32), C.c_void_p]),
     "bw_bfs_run_learned": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.POINTER(SwitchConfig), C.c_uint32,
                                      C.c_void_p, C.c_int, C.c_uint32, C.POINTER(BfsResult),
                                      C.POINTER(BfsLevelStats), C.c_uint32, C.c_void_p]),

@@ -131,6 +131,11 @@ namespace bw {
 
 int ensure_bfs_scratch(bw_context *ctx, uint64_t n, uint64_t m);
 int ensure_outdeg(bw_context *ctx, const bw_graph_view *g, cudaStream_t s);
+int pagerank_run_schedule_loop(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
+                               uint32_t schedule_len, uint32_t iterations, float *ranks, int loop_mode,
+                               bw_pagerank_result *result, float *diffs, cudaStream_t stream);
+int pagerank_moments(bw_context *ctx, const bw_graph_view *g, float *ls, float *lq, float *lm, cudaStream_t s);
+void pagerank_feature_vector(const bw_graph_view *g, float ls, float lq, float lm, uint32_t iteration, float *x);
 int bfs_edgeless(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t root, int32_t *levels,
                  bw_bfs_result *result, bw_bfs_level_stats *stats, uint32_t stats_capacity, cudaStream_t s);
 int ensure_pr_scratch(bw_context *ctx, uint64_t n, uint32_t iterations);

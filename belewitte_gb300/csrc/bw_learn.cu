@@ -465,6 +465,66 @@ struct Plan {
 };
 
 }  // namespace
+// Per-block partial log-degree moments of offsets off[0..n]: sum, sum of
+// squares and max of log2(1 + degree), written to part[3 * block + 0..2]
+// (summed on the host in block order: deterministic).
+__global__ void __launch_bounds__(256) k_log_degree_moments(const uint32_t *__restrict__ off, uint64_t n,
+                                                            float *__restrict__ part)
+{
+    __shared__ float r[3][8];
+    float ls = 0.f, lq = 0.f, lm = 0.f;
+    for (uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; v < n; v += uint64_t(gridDim.x) * blockDim.x) {
+        const float l = __log2f(1.0f + static_cast<float>(off[v + 1] - off[v]));
+        ls += l; lq += l * l; lm = fmaxf(lm, l);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ls += __shfl_xor_sync(FULL_MASK, ls, o);
+        lq += __shfl_xor_sync(FULL_MASK, lq, o);
+        lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
+    }
+    const unsigned w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { r[0][w] = ls; r[1][w] = lq; r[2][w] = lm; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f, c = 0.f;
+        for (unsigned i = 0; i < blockDim.x / 32; i++) { a += r[0][i]; b += r[1][i]; c = fmaxf(c, r[2][i]); }
+        part[3 * blockIdx.x] = a;
+        part[3 * blockIdx.x + 1] = b;
+        part[3 * blockIdx.x + 2] = c;
+    }
+}
+
+// The log-degree moments of the view's in-degrees (out-degrees when it has
+// no reverse CSR): block partials summed on the host in block order.
+int pagerank_moments(bw_context *ctx, const bw_graph_view *g, float *ls, float *lq, float *lm, cudaStream_t s)
+{
+    if (!ctx || !g || g->vertex_count == 0 || g->vertex_count > 0xffffffffULL) return BW_ERR_INVALID_ARGUMENT;
+    const uint32_t *off = g->rev_vertices ? g->rev_vertices : g->fwd_vertices;
+    if (!off) return BW_ERR_MISSING_REPRESENTATION;
+    const unsigned blocks = static_cast<unsigned>(ctx->sm_count) * 2u;
+    float *part = nullptr;
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&part), blocks * 3 * sizeof(float), s));
+    k_log_degree_moments<<<blocks, 256, 0, s>>>(off, g->vertex_count, part);
+    const cudaError_t e = cudaGetLastError();
+    std::vector<float> h(blocks * 3);
+    if (e == cudaSuccess) cudaMemcpyAsync(h.data(), part, h.size() * sizeof(float), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(part, s);
+    BW_CUDA(e);
+    BW_CUDA(cudaStreamSynchronize(s));
+    *ls = *lq = *lm = 0.f;
+    for (unsigned b = 0; b < blocks; b++) { *ls += h[3 * b]; *lq += h[3 * b + 1]; *lm = std::max(*lm, h[3 * b + 2]); }
+    return BW_OK;
+}
+
+// A PageRank iteration's features: every vertex is active, so the whole
+// vertex set is the frontier and nothing is left unvisited; the iteration
+// index is the level.
+void pagerank_feature_vector(const bw_graph_view *g, float ls, float lq, float lm, uint32_t iteration, float *x)
+{
+    const double n = static_cast<double>(g->vertex_count), m = static_cast<double>(g->edge_count);
+    bwfeat::compute(n, m, ls, lq, lm, n, m, n, m, static_cast<double>(iteration), x);
+}
+
 // The frontier {root} before level 0, with the statistics the level kernels
 // accumulate (the same formula as the side-statistics initialisation).
 __global__ void k_bfs_root_stats(const uint32_t *outdeg, uint32_t root, LevelSlot *out)
@@ -504,6 +564,44 @@ int bw_mlp_predict_host(const float *params, uint32_t classes, const float *feat
     for (uint32_t i = 0; i < n; i++)
         mlp_forward_host(params, classes, features + static_cast<size_t>(i) * F, probs + static_cast<size_t>(i) * classes);
     return BW_OK;
+}
+
+int bw_pagerank_features(bw_context *ctx, const bw_graph_view *g, uint32_t iteration, float out[12], void *stream)
+{
+    if (!out) return BW_ERR_INVALID_ARGUMENT;
+    float ls = 0.f, lq = 0.f, lm = 0.f;
+    BW_TRY(pagerank_moments(ctx, g, &ls, &lq, &lm, as_stream(stream)));
+    pagerank_feature_vector(g, ls, lq, lm, iteration, out);
+    return BW_OK;
+}
+
+int bw_pagerank_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_config *sw,
+                            uint32_t iterations, float *ranks, int loop_mode, bw_pagerank_result *result,
+                            float *diffs, int32_t *schedule_out, void *stream)
+{
+    if (!ctx || !g || !sw || !sw->params || !sw->candidates || sw->classes < 2 || sw->classes > BW_MLP_MAX_CLASSES)
+        return BW_ERR_INVALID_ARGUMENT;
+    const uint32_t K = sw->classes;
+    if (sw->fallback < 0 || static_cast<uint32_t>(sw->fallback) >= K) return BW_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    std::vector<float> hp(param_count(K));
+    BW_CUDA(cudaMemcpyAsync(hp.data(), sw->params, hp.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    BW_CUDA(cudaStreamSynchronize(s));
+    float ls = 0.f, lq = 0.f, lm = 0.f;
+    BW_TRY(pagerank_moments(ctx, g, &ls, &lq, &lm, s));
+    // The features depend on the iteration index only, so the whole
+    // schedule is chosen before the run.
+    std::vector<int32_t> sched(std::max<uint32_t>(iterations, 1u));
+    for (uint32_t it = 0; it < sched.size(); it++) {
+        float x[F], probs[BW_MLP_MAX_CLASSES];
+        pagerank_feature_vector(g, ls, lq, lm, it, x);
+        mlp_forward_host(hp.data(), K, x, probs);
+        sched[it] = sw->candidates[pick(probs, K, sw->fallback, sw->threshold)];
+    }
+    if (schedule_out)
+        for (uint32_t it = 0; it < iterations; it++) schedule_out[it] = sched[it];
+    return pagerank_run_schedule_loop(ctx, g, sched.data(), static_cast<uint32_t>(sched.size()), iterations, ranks,
+                                      loop_mode, result, diffs, s);
 }
 
 int bw_bfs_frontier_stats(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32_t depth,

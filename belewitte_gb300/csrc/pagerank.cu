@@ -2109,6 +2109,20 @@ int bw_pagerank_run(bw_context *ctx, const bw_graph_view *g, int variant,
                         result, diffs, stream);
 }
 
+}  // extern "C"
+
+// A schedule run in either loop mode, with the per-iteration diffs (the
+// learned PageRank run's entry).
+int bw::pagerank_run_schedule_loop(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
+                                   uint32_t schedule_len, uint32_t iterations, float *ranks, int loop_mode,
+                                   bw_pagerank_result *result, float *diffs, cudaStream_t stream)
+{
+    return run_pagerank(ctx, g, schedule, schedule_len, iterations, ranks, nullptr, loop_mode, 0, nullptr, result,
+                        diffs, stream);
+}
+
+extern "C" {
+
 int bw_pagerank_run_schedule(bw_context *ctx, const bw_graph_view *g, const int32_t *schedule,
                              uint32_t schedule_len, uint32_t iterations, float *ranks,
                              const bw_launch_config *cfg, int time_iterations,

@@ -1,4 +1,5 @@
-"""Learned per-level variant switching for BFS: data, training, evaluation.
+"""Learned variant switching: per BFS level and per PageRank iteration.
+Data, training, evaluation.
 
 Pipeline (all compute on the GPU through the C ABI):
 
@@ -21,6 +22,13 @@ Pipeline (all compute on the GPU through the C ABI):
 
 The trained predictor ships as data/bfs_predictor.npz and is loaded by
 ``load_predictor``.
+
+PageRank (``--algo pagerank``): ``profile_pagerank`` times every div-class
+variant per iteration on the same graphs, with the 12 features of
+``bw_pagerank_features`` (the whole vertex set as the frontier, the
+iteration index as the level); the same dataset, training and scoring
+follow, and the predictor ships as data/pagerank_predictor.npz
+(``load_pagerank_predictor``, ``run_pagerank_learned``).
 """
 from __future__ import annotations
 
@@ -39,6 +47,12 @@ from ._abi import check
 CANDIDATES = ["edge-list-bulk", "rev-edge-list-bulk", "struct-edge-list-bulk", "rev-struct-edge-list-bulk",
               "vertex-pull-bulk", "vertex-pull-warp-bulk", "frontier-push", "frontier-pull"]
 PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "bfs_predictor.npz"
+# PageRank: every variant of the div semantics class (a schedule cannot mix
+# it with the nodiv variants, whose ranks differ by construction)
+PR_CANDIDATES = ["edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list", "vertex-push",
+                 "vertex-pull", "vertex-push-warp", "vertex-pull-warp", "pull-segmented"]
+PR_PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "pagerank_predictor.npz"
+PR_PROFILE_ITERATIONS = 3
 TAU = 0.15
 
 
@@ -234,6 +248,67 @@ def predict(ctx, params, X, K):
 
 
 # ---------------------------------------------------------------------------
+# PageRank: per-iteration timings and features
+# ---------------------------------------------------------------------------
+def pagerank_features(ctx, g, iteration: int):
+    """The 12 features of PageRank iteration `iteration` (bw_pagerank_features)."""
+    import torch
+    out = (C.c_float * 12)()
+    st = torch.cuda.current_stream(g.device)
+    check(library().bw_pagerank_features(ctx.handle, C.byref(g.view), iteration, out, C.c_void_p(st.cuda_stream)),
+          "bw_pagerank_features")
+    return np.frombuffer(out, np.float32).copy()
+
+
+def profile_pagerank(ctx, g, candidates=PR_CANDIDATES, iterations: int = PR_PROFILE_ITERATIONS):
+    """(iteration_ms[I][K], features[I][12]): every candidate run alone for
+    `iterations` iterations after a warm-up run, timed per iteration with
+    CUDA events (pagerank_schedule)."""
+    from . import pagerank, pagerank_schedule
+    times = np.zeros((iterations, len(candidates)), np.float32)
+    for k, v in enumerate(candidates):
+        pagerank(ctx, g, v, 1)
+        run = pagerank_schedule(ctx, g, [v], iterations, time_iterations=True)
+        times[:, k] = np.asarray(run.iteration_ms[:iterations], np.float32)
+    feats = np.stack([pagerank_features(ctx, g, it) for it in range(iterations)])
+    return times, feats
+
+
+def collect_pagerank(ctx, specs, log=print):
+    import torch
+    records = []
+    for i, spec in enumerate(specs):
+        t0 = time.time()
+        g = spec.build(device=ctx.device)
+        records.append(profile_pagerank(ctx, g))
+        log(f"[{i + 1}/{len(specs)}] {spec.name()} N={g.vertex_count} M={g.edge_count} ({time.time() - t0:.1f}s)")
+        del g
+        torch.cuda.empty_cache()
+    return records
+
+
+def run_pagerank_learned(ctx, g, predictor: "Predictor", iterations: int = 30, *, ranks=None, loop: str = "host"):
+    """PageRank with the learned per-iteration choice
+    (bw_pagerank_run_learned); returns (PageRankRun, schedule of names)."""
+    import torch
+    from . import PageRankRun, pagerank_variant_names
+    if ranks is None:
+        ranks = torch.empty(g.vertex_count, dtype=torch.float32, device=g.device)
+    cfg = predictor.switch_config(pagerank=True)
+    res = _abi.PagerankResult()
+    diffs = (C.c_float * max(iterations, 1))()
+    sched = (C.c_int32 * max(iterations, 1))()
+    st = torch.cuda.current_stream(g.device)
+    check(library().bw_pagerank_run_learned(ctx.handle, C.byref(g.view), C.byref(cfg), iterations,
+                                            C.c_void_p(ranks.data_ptr()), 1 if loop == "graph" else 0, C.byref(res),
+                                            diffs, sched, C.c_void_p(st.cuda_stream)), "bw_pagerank_run_learned")
+    names = pagerank_variant_names()
+    run = PageRankRun(ranks, res.iterations, res.device_ms, list(diffs)[:iterations],
+                      kernel_launches=res.kernel_launches)
+    return run, [names[v] for v in list(sched)[:iterations]]
+
+
+# ---------------------------------------------------------------------------
 # scoring
 # ---------------------------------------------------------------------------
 def choose(probs, fallback: int, threshold: float):
@@ -270,10 +345,13 @@ class Predictor:
     fallback: int
     threshold: float
 
-    def switch_config(self, mlp_only: bool = False):
+    def switch_config(self, mlp_only: bool = False, pagerank: bool = False):
         """bw_switch_config; mlp_only sets BW_SWITCH_MLP_ONLY (the device
-        loop then leaves cluster-sized frontiers to the MLP too)."""
-        ids = (C.c_int32 * len(self.candidates))(*[bfs_variant_id(c) for c in self.candidates])
+        loop then leaves cluster-sized frontiers to the MLP too); pagerank:
+        the candidates are PageRank variant names."""
+        from . import pagerank_variant_id
+        vid = pagerank_variant_id if pagerank else bfs_variant_id
+        ids = (C.c_int32 * len(self.candidates))(*[vid(c) for c in self.candidates])
         cfg = _abi.SwitchConfig(C.c_void_p(self.params.data_ptr()), len(self.candidates), self.fallback, ids,
                                 self.threshold, 1 if mlp_only else 0)
         cfg._keep = ids
@@ -285,6 +363,10 @@ def save_predictor(path, params, candidates, fallback, threshold, meta=None):
     path.parent.mkdir(parents=True, exist_ok=True)
     np.savez(path, params=params.detach().cpu().numpy(), candidates=np.array(candidates),
              fallback=np.int64(fallback), threshold=np.float32(threshold), meta=json.dumps(meta or {}))
+
+
+def load_pagerank_predictor(path=PR_PREDICTOR_PATH, device: int = 0) -> Predictor:
+    return load_predictor(path, device)
 
 
 def load_predictor(path=PREDICTOR_PATH, device: int = 0) -> Predictor:
@@ -340,27 +422,32 @@ def main(argv=None):
     import argparse
     import torch
     from . import Context
-    ap = argparse.ArgumentParser(description="train the BFS variant predictor")
+    ap = argparse.ArgumentParser(description="train the BFS (per level) or PageRank (per iteration) variant predictor")
+    ap.add_argument("--algo", choices=["bfs", "pagerank"], default="bfs")
     ap.add_argument("--train", type=int, default=240)
     ap.add_argument("--heldout", type=int, default=40)
     ap.add_argument("--max-scale", type=int, default=23)
     ap.add_argument("--max-side", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--threshold", type=float, default=0.35)
-    ap.add_argument("--out", default=str(PREDICTOR_PATH))
+    ap.add_argument("--out", default="")
     ap.add_argument("--report", default="")
     args = ap.parse_args(argv)
     ctx = Context(0)
+    pr = args.algo == "pagerank"
+    cands = PR_CANDIDATES if pr else CANDIDATES
+    out_path = args.out or str(PR_PREDICTOR_PATH if pr else PREDICTOR_PATH)
+    gather = collect_pagerank if pr else collect
     train_specs = catalogue(args.train, seed=2024, max_scale=args.max_scale, max_side=args.max_side)
     held_specs = catalogue(args.heldout, seed=4048, max_scale=args.max_scale, max_side=args.max_side)
     t0 = time.time()
-    recs = collect(ctx, train_specs)
-    held = collect(ctx, held_specs)
+    recs = gather(ctx, train_specs)
+    held = gather(ctx, held_specs)
     X, T, W = build_dataset(recs)
     params, curve = train(ctx, X, T, W, steps=args.steps)
     fb = fallback_variant(recs)
-    K = len(CANDIDATES)
-    report = {"candidates": CANDIDATES, "fallback": CANDIDATES[fb], "threshold": args.threshold,
+    K = len(cands)
+    report = {"algo": args.algo, "candidates": cands, "fallback": cands[fb], "threshold": args.threshold,
               "train_samples": int(len(X)), "loss_curve": curve, "collect_s": time.time() - t0}
     for label, rs, specs in (("train", recs, train_specs), ("heldout", held, held_specs)):
         tot = {"oracle_best": 0.0, "best_fixed": 0.0, "chosen": 0.0, "fallback_only": 0.0}
@@ -377,8 +464,8 @@ def main(argv=None):
         report[label] = {"totals_ms": tot, "speedup_vs_best_fixed": tot["best_fixed"] / tot["chosen"],
                          "speedup_vs_fallback": tot["fallback_only"] / tot["chosen"],
                          "efficiency_vs_oracle_best": tot["oracle_best"] / tot["chosen"], "graphs": per}
-    save_predictor(args.out, params, CANDIDATES, fb, args.threshold,
-                   meta={"train_graphs": [s.name() for s in train_specs], "steps": args.steps})
+    save_predictor(out_path, params, cands, fb, args.threshold,
+                   meta={"algo": args.algo, "train_graphs": [s.name() for s in train_specs], "steps": args.steps})
     if args.report:
         Path(args.report).write_text(json.dumps(report, indent=1))
     print(json.dumps({k: report[k] for k in ("fallback", "train_samples")} |

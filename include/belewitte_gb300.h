@@ -514,6 +514,37 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g,
                        bw_bfs_result *result, bw_bfs_level_stats *stats,
                        uint32_t stats_capacity, void *stream);
 
+/*
+ * The 12 features of PageRank iteration `iteration` (bw_bfs_features with
+ * every vertex active: the frontier is the whole vertex set, N vertices and
+ * M edges, with the log-degree moments of the in-degrees -- the
+ * out-degrees when the view has no reverse CSR -- nothing unvisited, and
+ * the iteration index as the level).  out: host, 12 floats.
+ */
+int bw_pagerank_features(bw_context *ctx, const bw_graph_view *g,
+                         uint32_t iteration, float out[12], void *stream);
+
+/*
+ * PageRank whose every iteration runs the variant the MLP picks from that
+ * iteration's features (above), the fallback below the confidence
+ * threshold.  The features depend on the iteration index only, so the
+ * whole schedule is chosen before the run, which then runs as
+ * bw_pagerank_run_schedule does (loop_mode as in bw_pagerank_run).  The
+ * candidates must share one semantics class (all div or all nodiv
+ * variants).  diffs (optional, host, `iterations` floats) as in
+ * bw_pagerank_run; schedule_out (optional, host, `iterations` entries)
+ * receives the variant chosen for each iteration.  It plays the part of
+ * the reference's PageRank `switch` implementation
+ * (pagerank/pagerank.cpp:174-358), which picks its kernel through a
+ * predictor library.
+ */
+int bw_pagerank_run_learned(bw_context *ctx, const bw_graph_view *g,
+                            const bw_switch_config *sw, uint32_t iterations,
+                            float *ranks, int loop_mode,
+                            bw_pagerank_result *result, float *diffs,
+                            int32_t *schedule_out, void *stream);
+
+
 /* ------------------------------------------------------------------------ */
 /* Batched persistent traversal                                              */
 /* ------------------------------------------------------------------------ */

@@ -167,3 +167,66 @@ def test_learned_graph_loop_without_level_log(ctx):
             run = learn.run_learned(ctx, g, pred, r, loop="graph", stats=stats)
             assert np.array_equal(run.levels.cpu().numpy(), lv), (name, stats)
             assert run.level_count == len(cnt), (name, stats)
+
+
+# ---------------------------------------------------------------------------
+# PageRank: per-iteration variant choice
+# ---------------------------------------------------------------------------
+def _quick_pr_predictor(ctx):
+    """A PageRank predictor trained on a few small graphs (fast)."""
+    specs = learn.catalogue(8, seed=11, max_scale=15, max_side=600)
+    recs = learn.collect_pagerank(ctx, specs, log=lambda *a: None)
+    X, T, W = learn.build_dataset(recs)
+    params, _ = learn.train(ctx, X, T, W, steps=1500)
+    return learn.Predictor(params, learn.PR_CANDIDATES, learn.fallback_variant(recs), 0.3), recs
+
+
+def test_pagerank_features_are_whole_graph_moments(ctx):
+    h = catalog()["rmat14"][0]()
+    g = bw.DeviceGraph(h)
+    deg = np.diff(h.rev_vertices.astype(np.int64))
+    l = np.log2(1.0 + deg)
+    want = np.zeros(12, np.float32)
+    lib = bw.library()
+    for it in (0, 1, 7):
+        f = learn.pagerank_features(ctx, g, it)
+        x = (C.c_float * 12)()
+        lib.bw_bfs_features(h.vertex_count, h.edge_count, float(l.sum()), float((l * l).sum()), float(l.max()),
+                            h.vertex_count, h.edge_count, h.vertex_count, h.edge_count, it, x)
+        want[:] = np.frombuffer(x, np.float32)
+        assert np.allclose(f, want, rtol=1e-4, atol=1e-5), (it, f, want)
+
+
+def test_learned_pagerank_within_tolerance(ctx):
+    """Ranks of the learned per-iteration schedule against the oracle of the
+    div semantics: the same bar as every order-changing variant."""
+    pred, _ = _quick_pr_predictor(ctx)
+    allowed = set(learn.PR_CANDIDATES)
+    for name in ["rmat14", "er", "grid", "ba", "star", "tiny", "isolated"]:
+        h = catalog()[name][0]()
+        g = bw.DeviceGraph(h)
+        ref, _ = oracle.pagerank(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 12)
+        r64 = oracle.pagerank_f64(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 12)
+        for loop in ("host", "graph"):
+            run, sched = learn.run_pagerank_learned(ctx, g, pred, 12, loop=loop)
+            got = run.ranks.cpu().numpy().astype(np.float64)
+            assert len(sched) == 12 and set(sched) <= allowed, sched
+            assert float((np.abs(got - ref) / np.abs(ref)).max()) <= 1e-5, (name, loop)
+            assert float((np.abs(got - r64) / np.abs(r64)).max()) <= 1e-4, (name, loop)
+
+
+def test_learned_pagerank_choices_score(ctx):
+    """On its recorded timings the trained network's schedule costs no more
+    than the fixed fallback variant's (what the network adds to the plain
+    method), and every schedule is scored against the oracle-best one."""
+    pred, recs = _quick_pr_predictor(ctx)
+    K = len(learn.PR_CANDIDATES)
+    chosen = fallback = best = 0.0
+    for times, feats in recs:
+        probs = learn.predict(ctx, pred.params, feats, K)
+        ch = learn.choose(probs, pred.fallback, pred.threshold)
+        sc = learn.score_graph(times, ch)
+        chosen += sc["chosen"]
+        fallback += float(times[:, pred.fallback].sum())
+        best += sc["oracle_best"]
+    assert best <= chosen <= fallback * 1.02, (best, chosen, fallback)
