@@ -517,12 +517,13 @@ int pagerank_moments(bw_context *ctx, const bw_graph_view *g, float *ls, float *
 }
 
 // A PageRank iteration's features: every vertex is active, so the whole
-// vertex set is the frontier and nothing is left unvisited; the iteration
-// index is the level.
+// vertex set is the frontier and nothing is left unvisited.  The level
+// separates the first iteration (0) from the rest (1): after the first, an
+// iteration does the same work every time.
 void pagerank_feature_vector(const bw_graph_view *g, float ls, float lq, float lm, uint32_t iteration, float *x)
 {
     const double n = static_cast<double>(g->vertex_count), m = static_cast<double>(g->edge_count);
-    bwfeat::compute(n, m, ls, lq, lm, n, m, n, m, static_cast<double>(iteration), x);
+    bwfeat::compute(n, m, ls, lq, lm, n, m, n, m, iteration == 0 ? 0.0 : 1.0, x);
 }
 
 // The frontier {root} before level 0, with the statistics the level kernels

@@ -24,11 +24,12 @@ The trained predictor ships as data/bfs_predictor.npz and is loaded by
 ``load_predictor``.
 
 PageRank (``--algo pagerank``): ``profile_pagerank`` times every div-class
-variant per iteration on the same graphs, with the 12 features of
-``bw_pagerank_features`` (the whole vertex set as the frontier, the
-iteration index as the level); the same dataset, training and scoring
-follow, and the predictor ships as data/pagerank_predictor.npz
-(``load_pagerank_predictor``, ``run_pagerank_learned``).
+variant per iteration on the same graph specs, with R-MAT and ER left
+directed, and with the 12 features of ``bw_pagerank_features`` (the whole
+vertex set as the frontier; the level separates the first iteration from
+the rest); the same dataset, training and scoring follow, and the
+predictor ships as data/pagerank_predictor.npz (``load_pagerank_predictor``,
+``run_pagerank_learned``).
 """
 from __future__ import annotations
 
@@ -52,7 +53,8 @@ PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "bfs_predictor.npz"
 PR_CANDIDATES = ["edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list", "vertex-push",
                  "vertex-pull", "vertex-push-warp", "vertex-pull-warp", "pull-segmented"]
 PR_PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "pagerank_predictor.npz"
-PR_PROFILE_ITERATIONS = 3
+PR_PROFILE_ITERATIONS = 8      # timed per candidate: the first iteration, then the steady state
+PR_RUN_ITERATIONS = 30         # the run a profile stands for
 TAU = 0.15
 
 
@@ -69,15 +71,17 @@ class GraphSpec:
         p = ",".join(f"{k}={v}" for k, v in sorted(self.params.items()))
         return f"{self.kind}({p};seed={self.seed})"
 
-    def build(self, device: int = 0, reps: int = 63):
+    def build(self, device: int = 0, reps: int = 63, symmetrise: bool = True):
+        """The graph; R-MAT and ER are symmetrised unless `symmetrise` is
+        False (grids and BA are symmetric by construction)."""
         from . import DeviceGraph
         p = dict(self.params)
         if self.kind == "rmat":
             return DeviceGraph.generate("rmat", scale=p["scale"], edge_factor=p["edge_factor"], a=p["a"],
-                                        b=p["b"], c=p["c"], seed=self.seed, symmetrise=True, device=device,
+                                        b=p["b"], c=p["c"], seed=self.seed, symmetrise=symmetrise, device=device,
                                         reps=reps)
         if self.kind == "er":
-            return DeviceGraph.generate("er", n=p["n"], m=p["m"], seed=self.seed, symmetrise=True,
+            return DeviceGraph.generate("er", n=p["n"], m=p["m"], seed=self.seed, symmetrise=symmetrise,
                                         device=device, reps=reps)
         if self.kind == "grid":
             return DeviceGraph.generate("grid", h=p["side"], w=p["side"], device=device, reps=reps)
@@ -260,17 +264,24 @@ def pagerank_features(ctx, g, iteration: int):
     return np.frombuffer(out, np.float32).copy()
 
 
-def profile_pagerank(ctx, g, candidates=PR_CANDIDATES, iterations: int = PR_PROFILE_ITERATIONS):
-    """(iteration_ms[I][K], features[I][12]): every candidate run alone for
-    `iterations` iterations after a warm-up run, timed per iteration with
-    CUDA events (pagerank_schedule)."""
+def profile_pagerank(ctx, g, candidates=PR_CANDIDATES, iterations: int = PR_PROFILE_ITERATIONS,
+                     run_iterations: int = PR_RUN_ITERATIONS):
+    """(ms[2][K], features[2][12]) for a `run_iterations`-iteration run:
+    row 0 the first iteration, row 1 the other run_iterations - 1 at the
+    steady-state rate (median of the last half of `iterations` timed
+    iterations: some variants settle after the first few, e.g.
+    pull-segmented takes its hub-first order).  Every candidate runs alone
+    after a warm-up run, timed per iteration with CUDA events
+    (pagerank_schedule)."""
     from . import pagerank, pagerank_schedule
-    times = np.zeros((iterations, len(candidates)), np.float32)
+    times = np.zeros((2, len(candidates)), np.float32)
     for k, v in enumerate(candidates):
         pagerank(ctx, g, v, 1)
         run = pagerank_schedule(ctx, g, [v], iterations, time_iterations=True)
-        times[:, k] = np.asarray(run.iteration_ms[:iterations], np.float32)
-    feats = np.stack([pagerank_features(ctx, g, it) for it in range(iterations)])
+        t = np.asarray(run.iteration_ms[:iterations], np.float64)
+        times[0, k] = t[0]
+        times[1, k] = np.median(t[iterations // 2:]) * (run_iterations - 1)
+    feats = np.stack([pagerank_features(ctx, g, it) for it in (0, 1)])
     return times, feats
 
 
@@ -279,7 +290,7 @@ def collect_pagerank(ctx, specs, log=print):
     records = []
     for i, spec in enumerate(specs):
         t0 = time.time()
-        g = spec.build(device=ctx.device)
+        g = spec.build(device=ctx.device, symmetrise=False)    # PageRank runs on directed graphs
         records.append(profile_pagerank(ctx, g))
         log(f"[{i + 1}/{len(specs)}] {spec.name()} N={g.vertex_count} M={g.edge_count} ({time.time() - t0:.1f}s)")
         del g

@@ -14,6 +14,9 @@ The same JSON line carries:
     sources of the giant component -- the learned per-level switch (shipped
     predictor, device-side decisions in a CUDA graph) against every fixed
     candidate variant; depths are checked identical.
+  * learned_pagerank: the learned per-iteration PageRank choice (shipped
+    predictor) against every fixed div-class variant, 30 iterations, on the
+    headline R-MAT graph and a 4096 x 4096 grid.
   * batched: many graphs (BFS + 20-iteration PageRank each) and many BFS
     sources, each in one persistent launch.
   * roofline of the dominant PageRank kernel, e2e through the C ABI with
@@ -209,6 +212,37 @@ def bfs_learned_vs_fixed(ctx, dev):
     return out
 
 
+def pagerank_learned_vs_fixed(ctx, dev):
+    """The learned per-iteration PageRank choice against every fixed
+    div-class variant, 30 iterations each, device-timed (CUDA events around
+    the run), on the headline R-MAT graph and a 4096 x 4096 grid."""
+    import torch
+
+    import belewitte_gb300 as bw
+    from belewitte_gb300 import learn
+    pred = learn.load_pagerank_predictor(device=dev)
+    out = {}
+    for label, kind, kw in ((f"R-MAT scale {SCALE} edge factor {EDGE_FACTOR} seed {SEED}", "rmat",
+                             dict(scale=SCALE, edge_factor=EDGE_FACTOR, seed=SEED)),
+                            ("grid 4096 x 4096", "grid", dict(h=4096, w=4096))):
+        g = bw.DeviceGraph.generate(kind, device=dev, reps=63, **kw)
+        ranks = torch.empty(g.vertex_count, dtype=torch.float32, device=f"cuda:{dev}")
+        times = {}
+        for v in learn.PR_CANDIDATES:
+            bw.pagerank(ctx, g, v, 2, ranks=ranks)
+            times[v] = bw.pagerank(ctx, g, v, ITERATIONS, ranks=ranks).device_ms
+        learn.run_pagerank_learned(ctx, g, pred, 2, ranks=ranks)
+        run, sched = learn.run_pagerank_learned(ctx, g, pred, ITERATIONS, ranks=ranks)
+        best = min(times, key=times.get)
+        out[label] = {"learned_ms": round(run.device_ms, 3), "learned_schedule": sorted(set(sched)),
+                      "best_fixed_variant": best, "best_fixed_ms": round(times[best], 3),
+                      "speedup_vs_best_fixed": round(times[best] / run.device_ms, 3),
+                      "ms_fixed": {k: round(v, 3) for k, v in times.items()}}
+        del g, ranks
+        torch.cuda.empty_cache()
+    return out
+
+
 def batched(ctx, dev, graphs: int):
     import torch
 
@@ -390,6 +424,7 @@ def run_ours(args):
     extras = {}
     if not args.no_bfs:
         extras["learned_switch"] = bfs_learned_vs_fixed(ctx, dev)
+        extras["learned_pagerank"] = pagerank_learned_vs_fixed(ctx, dev)
     if not args.no_batched:
         extras["batched"] = batched(ctx, dev, args.batch_graphs)
     cpu = None

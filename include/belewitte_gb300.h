@@ -519,7 +519,8 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g,
  * every vertex active: the frontier is the whole vertex set, N vertices and
  * M edges, with the log-degree moments of the in-degrees -- the
  * out-degrees when the view has no reverse CSR -- nothing unvisited, and
- * the iteration index as the level).  out: host, 12 floats.
+ * level 0 for the first iteration, 1 for every later one, which all do the
+ * same work).  out: host, 12 floats.
  */
 int bw_pagerank_features(bw_context *ctx, const bw_graph_view *g,
                          uint32_t iteration, float out[12], void *stream);
@@ -527,8 +528,8 @@ int bw_pagerank_features(bw_context *ctx, const bw_graph_view *g,
 /*
  * PageRank whose every iteration runs the variant the MLP picks from that
  * iteration's features (above), the fallback below the confidence
- * threshold.  The features depend on the iteration index only, so the
- * whole schedule is chosen before the run, which then runs as
+ * threshold.  The features separate only the first iteration from the
+ * rest, so the whole schedule is chosen before the run, which then runs as
  * bw_pagerank_run_schedule does (loop_mode as in bw_pagerank_run).  The
  * candidates must share one semantics class (all div or all nodiv
  * variants).  diffs (optional, host, `iterations` floats) as in
