@@ -118,16 +118,18 @@ def build_plugins(force: bool = False) -> list[Path]:
         out.append(target)
     with _cf.ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(_run, steps))
-    # the shipped learned predictor as a reference-format predictor library
-    # (kernel-runner -a bfs -k switch -m libbfs_mlp_predictor.so)
+    # the shipped learned predictors as reference-format predictor libraries
+    # (kernel-runner -a bfs|pagerank -k switch -m lib{bfs,pagerank}_mlp_predictor.so)
     import importlib.util
     spec = importlib.util.spec_from_file_location("_bw_predictor_export", PKG / "predictor_export.py")
     pe = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(pe)
-    if pe.DEFAULT_NPZ.exists():
-        if force or _stale(pe.DEFAULT_SO, [pe.DEFAULT_NPZ, Path(pe.__file__), LIB] + list(INCLUDE.glob("*.h"))):
-            pe.export_predictor()
-        out.append(pe.DEFAULT_SO)
+    for npz, so, name, algo in ((pe.DEFAULT_NPZ, pe.DEFAULT_SO, "bfs-mlp", "bfs"),
+                                (pe.PAGERANK_NPZ, pe.PAGERANK_SO, "pagerank-mlp", "pagerank")):
+        if npz.exists():
+            if force or _stale(so, [npz, Path(pe.__file__), LIB] + list(INCLUDE.glob("*.h"))):
+                pe.export_predictor(so, npz, name, algo)
+            out.append(so)
     return out
 
 

@@ -9,6 +9,7 @@
 // `vertex \t rank` with digits10 + 1 significant digits, otherwise the
 // vertex ids ordered by rank with the low 16 mantissa bits masked and each
 // 1000-entry bucket re-sorted by id (pagerank.cpp:142-168).
+#include <cmath>
 #include <algorithm>
 #include <cstring>
 #include <iomanip>
@@ -122,9 +123,17 @@ class PageRankImplementation : public PageRankBase {
 
 // `switch`: the predictor picks one variant per run from the graph
 // properties (pagerank/pagerank.cpp:98-100 calls predictInitial only).
+// Beside the reference's graph properties it publishes the in-degree log
+// moments (sum, sum of squares and max of log2(1 + in-degree)), which the
+// learned PageRank predictor reads.
 class PageRankSwitch : public PageRankBase, public SwitchBase {
   public:
-    PageRankSwitch() : SwitchBase(options, false) {}
+    PageRankSwitch() : SwitchBase(options, false)
+    {
+        log_sum_ = &add_graph_prop("in log degree sum");
+        log_sq_sum_ = &add_graph_prop("in log degree square sum");
+        log_max_ = &add_graph_prop("in log degree max");
+    }
 
   protected:
     void prepareRun() override
@@ -132,7 +141,23 @@ class PageRankSwitch : public PageRankBase, public SwitchBase {
         setup_switch([](const std::string &n) { return bw_pagerank_variant_lookup(n.c_str()); }, "edge-list");
     }
     void cleanupRun() override { close(); }
-    void after_load() override { set_graph_props(graph_.host); }
+    void after_load() override
+    {
+        set_graph_props(graph_.host);
+        const bw_host_graph &h = graph_.host;
+        const uint32_t *off = h.rev_vertices ? h.rev_vertices : h.fwd_vertices;
+        double ls = 0.0, lq = 0.0, lm = 0.0;
+        for (uint64_t v = 0; off && v < h.vertex_count; v++) {
+            const double l = std::log2(1.0 + static_cast<double>(off[v + 1] - off[v]));
+            ls += l;
+            lq += l * l;
+            lm = std::max(lm, l);
+        }
+        *log_sum_ = ls;
+        *log_sq_sum_ = lq;
+        *log_max_ = lm;
+    }
+    prop_ref *log_sum_, *log_sq_sum_, *log_max_;
     void runImplementation(std::ofstream &out) override { run(out, [this] { return predict_initial(); }); }
 };
 

@@ -134,6 +134,73 @@ def test_predict_host_rejects_bad_arguments():
     assert lib.bw_mlp_predict_host(p, 17, x, 1, p) != 0
 
 
+def test_exported_pagerank_lookup_matches_host_forward(predictor_so, tmp_path):
+    """The PageRank predictor library picks what bw_mlp_predict_host picks
+    on the steady-state iteration's features of the given graph moments."""
+    d = np.load(pe.PAGERANK_NPZ, allow_pickle=False)
+    params = d["params"].astype(np.float32)
+    cands = [str(c) for c in d["candidates"]]
+    K, fb, thr = len(cands), int(d["fallback"]), float(d["threshold"])
+    exe = _driver(tmp_path)
+    rng = np.random.default_rng(3)
+    rows = []
+    for _ in range(200):
+        n = int(2 ** rng.uniform(10, 24))
+        m = int(n * 2 ** rng.uniform(1, 5))
+        mean = rng.uniform(0.5, 6.0)
+        ls = n * mean
+        lq = n * (mean * mean + rng.uniform(0.0, 4.0))
+        rows.append([n, m, ls, lq, mean + rng.uniform(1.0, 14.0)])
+    text = "\n".join(" ".join(repr(float(x)) for x in r) for r in rows) + "\n"
+    out = subprocess.run([str(exe), str(pe.PAGERANK_SO), *pe.PAGERANK_PROPERTIES], input=text, capture_output=True,
+                         text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.splitlines()
+    assert lines[0] == f"name pagerank-mlp default {fb}"
+    picks = [int(ln.split()[1]) for ln in lines[1 + K:]]
+    lib = bw.library()
+    cp = params.ctypes.data_as(C.POINTER(C.c_float))
+    expect = []
+    for n, m, ls, lq, lm in rows:
+        x = (C.c_float * 12)()
+        lib.bw_bfs_features(int(n), int(m), ls, lq, lm, int(n), int(m), int(n), int(m), 1, x)
+        p = (C.c_float * K)()
+        _abi.check(lib.bw_mlp_predict_host(cp, K, x, 1, p), "bw_mlp_predict_host")
+        p = np.frombuffer(p, np.float32)
+        expect.append(fb if p.max() < thr else int(p.argmax()))
+    assert picks == expect
+
+
+@pytest.mark.gpu
+def test_kernel_runner_pagerank_switch_with_exported_predictor(predictor_so, tmp_path):
+    """kernel-runner -a pagerank -k switch -m libpagerank_mlp_predictor.so:
+    ranks within the order-changing variants' tolerance, and the variant
+    the learned run chooses for its steady-state iterations."""
+    from belewitte_gb300 import learn
+    import oracle
+    for name, h in (("rmat", bw.HostGraph.rmat(14, 16, seed=9)), ("grid", bw.HostGraph.grid(300, 300))):
+        p = tmp_path / f"{name}.graph"
+        h.write(p)
+        log = tmp_path / f"{name}.log"
+        runner = PKG / "kernel-runner"
+        out = subprocess.run([str(runner), "-L", str(PKG), "-a", "pagerank", "-k", "switch", "-m",
+                              str(pe.PAGERANK_SO), "-l", str(log), "-i", "30", "--validate", "-o", str(tmp_path),
+                              str(p)], capture_output=True, text=True, timeout=600)
+        assert out.returncode == 0, out.stderr
+        preds = [int(ln.split(":")[2]) for ln in log.read_text().splitlines() if ln.startswith("prediction:")]
+        assert len(preds) == 1
+        pred = learn.load_pagerank_predictor()
+        run, sched = learn.run_pagerank_learned(ctx_of(), bw.DeviceGraph(h), pred, 30)
+        assert pred.candidates[preds[0]] == sched[1], (name, pred.candidates[preds[0]], sched)
+        ref, _ = oracle.pagerank(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 30)
+        got = np.loadtxt(tmp_path / f"{name}.output", dtype=np.float64)[:, 1]
+        assert float((np.abs(got - ref) / np.abs(ref)).max()) <= 2e-5, name
+
+
+def ctx_of():
+    return bw.Context()
+
+
 @pytest.mark.gpu
 def test_kernel_runner_switch_with_exported_predictor(predictor_so, tmp_path):
     import torch
