@@ -1,4 +1,5 @@
-"""Launch-geometry autotuner for the BFS and PageRank variants.
+"""Launch-geometry and push/pull-threshold autotuner for the BFS and
+PageRank variants and the batched launch.
 
 The reference fixes its geometry with Backend::computeDivision
 (Backend.cpp:52-70) and takes the virtual-warp width and chunk of the warp
@@ -9,6 +10,12 @@ virtual-warp width and chunk -- on the device, and keeps the fastest per
 (algorithm, variant, graph shape class) in a JSON cache.  Results are
 identical for every configuration (BFS depths bit-exact, PageRank within
 the variant's tolerance), so tuning changes time only.
+
+The batched launch (bw_batch_run) switches each BFS level between
+top-down and bottom-up by a divisor: bottom-up once the frontier holds more
+than 1/divisor of the unit's vertices.  ``tune_batch`` times the batched
+BFS over a range of divisors and keeps the fastest per mode and graph shape
+class; ``lookup_batch`` is what batch.run_graphs / run_sources use.
 """
 from __future__ import annotations
 
@@ -127,3 +134,58 @@ def lookup(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
         return sum(abs(x - y) for x, y in zip(a, b))
     near = min(entries, key=dist)
     return dict(entries[near]["config"])
+
+
+# ---------------------------------------------------------------------------
+# batched launch: the push/pull divisor
+# ---------------------------------------------------------------------------
+BU_DIVISORS = [4, 8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 1024, 2048]
+
+
+def tune_batch(ctx, run, key: str, *, divisors=BU_DIVISORS, repeats: int = 3, cache: Path | None = CACHE,
+               log=None):
+    """`run(bu_div)` runs one batched launch and returns its bw_batch_result;
+    keeps the divisor with the lowest median device time under
+    cache["batch"][key].  Depths are identical for every divisor (the level
+    direction changes how, not what, a level visits)."""
+    best = None
+    for d in divisors:
+        run(d)                                        # warm-up
+        ms = float(np.median([run(d).device_ms for _ in range(repeats)]))
+        if log:
+            log(f"batch {key} divisor {d}: {ms:.3f} ms")
+        if best is None or ms < best[1]:
+            best = (d, ms)
+    if cache is not None:
+        data = json.loads(cache.read_text()) if cache.exists() else {}
+        data.setdefault("batch", {})[key] = {"bu_div": best[0], "ms": best[1]}
+        cache.parent.mkdir(parents=True, exist_ok=True)
+        cache.write_text(json.dumps(data, indent=1, sort_keys=True))
+    return best
+
+
+def batch_key(mode: str, g=None) -> str:
+    """Cache key: the mode, and for many sources on one graph its shape class."""
+    return f"sources/{shape_class(g)}" if mode == "sources" and g is not None else mode
+
+
+def lookup_batch(mode: str, g=None, cache: Path = CACHE) -> int:
+    """The tuned divisor for this mode (and the nearest shape class of `g`
+    for sources), or 0 (the library default)."""
+    if not cache.exists():
+        return 0
+    entries = json.loads(cache.read_text()).get("batch", {})
+    key = batch_key(mode, g)
+    if key in entries:
+        return int(entries[key]["bu_div"])
+    if mode != "sources" or g is None:
+        return 0
+    cands = [k for k in entries if k.startswith("sources/")]
+    if not cands:
+        return 0
+    cls = [int(x[1:]) for x in shape_class(g).split("-")]
+
+    def dist(k: str) -> int:
+        other = [int(x[1:]) for x in k.split("/", 1)[1].split("-")]
+        return sum(abs(x - y) for x, y in zip(cls, other))
+    return int(entries[min(cands, key=dist)]["bu_div"])

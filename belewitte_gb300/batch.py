@@ -69,16 +69,21 @@ def pack(graphs: list[DeviceGraph], device: int = 0) -> PackedGraphs:
 
 
 def run_graphs(ctx, packed: PackedGraphs, pr_iterations: int = 20, levels=None, ranks=None, grid: int = 0,
-               stream=None):
-    """Workload A: per graph a BFS and a PageRank, in one persistent launch."""
+               stream=None, bu_div: int | None = None):
+    """Workload A: per graph a BFS and a PageRank, in one persistent launch.
+    bu_div: the push/pull divisor (None: the autotuner's, else the
+    library default)."""
     import torch
+    from . import autotune
+    if bu_div is None:
+        bu_div = autotune.lookup_batch("graphs")
     dev = packed.offsets.device
     if levels is None:
         levels = torch.empty(packed.vertex_count, dtype=torch.int32, device=dev)
     if ranks is None:
         ranks = torch.empty(packed.vertex_count, dtype=torch.float32, device=dev)
     res = _abi.BatchResult()
-    cfg = _abi.LaunchConfig(0, grid, 0, 0)
+    cfg = _abi.LaunchConfig(0, grid, 0, bu_div)
     st = stream or torch.cuda.current_stream(dev)
     check(library().bw_batch_run(ctx.handle, C.byref(packed.view), GRAPHS, _ptr(packed.offsets), packed.count,
                                  _ptr(packed.roots), _ptr(packed.order), packed.count, packed.max_vertices,
@@ -87,15 +92,20 @@ def run_graphs(ctx, packed: PackedGraphs, pr_iterations: int = 20, levels=None, 
     return levels, ranks, res
 
 
-def run_sources(ctx, g: DeviceGraph, sources, levels=None, grid: int = 0, stream=None):
-    """Workload B: BFS from every source of `sources` on graph `g`."""
+def run_sources(ctx, g: DeviceGraph, sources, levels=None, grid: int = 0, stream=None, bu_div: int | None = None):
+    """Workload B: BFS from every source of `sources` on graph `g`.
+    bu_div: the push/pull divisor (None: the autotuner's for g's shape
+    class, else the library default)."""
     import torch
+    from . import autotune
+    if bu_div is None:
+        bu_div = autotune.lookup_batch("sources", g)
     dev = g.device
     src = torch.as_tensor(np.asarray(sources, dtype=np.int32), device=dev)
     if levels is None:
         levels = torch.empty((len(sources), g.vertex_count), dtype=torch.int32, device=dev)
     res = _abi.BatchResult()
-    cfg = _abi.LaunchConfig(0, grid, 0, 0)
+    cfg = _abi.LaunchConfig(0, grid, 0, bu_div)
     st = stream or torch.cuda.current_stream(dev)
     check(library().bw_batch_run(ctx.handle, C.byref(g.view), SOURCES, None, 1, _ptr(src), None, len(sources),
                                  g.vertex_count, 0, _ptr(levels), None, C.byref(cfg), C.byref(res),

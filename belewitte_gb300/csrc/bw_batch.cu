@@ -33,7 +33,7 @@ constexpr float DAMPING = 0.85f;
 constexpr uint32_t BATCH_PR_LIGHT = 64;   // PageRank rows above this are summed by a whole warp
 constexpr int BATCH_PR_UNROLL = 8;
 constexpr int BATCH_BFS_UNROLL = 4;
-constexpr uint32_t BATCH_BU_DIV = 24;     // bottom-up levels: frontier above 1/24 of the unit
+constexpr uint32_t BATCH_BU_DIV = 24;     // default push/pull divisor: bottom-up above 1/24 of the unit
 constexpr uint32_t BATCH_PR_L = 8;        // warp sums: windows of 32 x 8 terms
 
 struct BatchArgs {
@@ -51,6 +51,7 @@ struct BatchArgs {
     float *ranks;
     uint32_t pr_iters;
     uint32_t vis_words;       // > 0: the unit's visited set is a shared-memory bitmap of this many words
+    uint32_t bu_div;          // a level whose frontier holds more than 1/bu_div of the unit runs bottom-up
     unsigned long long *traversed;
 };
 
@@ -135,14 +136,14 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(BatchArgs a)
                     qout[base + g.thread_rank()] = u;
                 }
             };
-            // A frontier above 1/BATCH_BU_DIV of the unit's vertices: bottom-up.
+            // A frontier above 1/bu_div of the unit's vertices: bottom-up.
             // Every vertex not yet reached looks for an in-neighbour reached
             // before this level, which is then at `depth` (one at a smaller
             // depth would have reached it already); the bitmap answers, and
             // is updated only once the level is done, so that it reads as of
             // the level's start.
             const uint32_t nunit = ve - vb;
-            const bool bottom_up = bitmap && a.rev_v && len > nunit / BATCH_BU_DIV;
+            const bool bottom_up = bitmap && a.rev_v && len > nunit / a.bu_div;
             if (bottom_up) {
                 const uint32_t words = (nunit + 31) / 32;
                 for (uint32_t w = tid; w < words; w += BATCH_THREADS) {
@@ -390,6 +391,7 @@ extern "C" int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode, c
     a.ranks = ranks;
     a.pr_iters = mode == BW_BATCH_GRAPHS ? pr_iterations : 0;
     a.vis_words = bitmap ? static_cast<uint32_t>(words) : 0u;
+    a.bu_div = (cfg && cfg->chunk_size) ? cfg->chunk_size : BATCH_BU_DIV;
     const size_t per_cta = static_cast<size_t>(2) * max_unit_vertices;
     char *scratch = nullptr;
     const size_t bytes = 64 + grid * per_cta * sizeof(uint32_t) + (a.pr_iters ? grid * per_cta * sizeof(float) : 0);

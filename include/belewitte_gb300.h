@@ -567,6 +567,10 @@ int bw_pagerank_run_learned(bw_context *ctx, const bw_graph_view *g,
  *   depths into levels[i * vertex_count + v].
  * graph_offsets, roots and `order` (unit ids, largest first; NULL = 0..n-1)
  * are device arrays.
+ * cfg (optional): grid_size (0: two CTAs per SM where they fit), block_size
+ * (0 or 512), and chunk_size as the push/pull divisor -- a BFS level whose
+ * frontier holds more than 1/chunk_size of the unit's vertices runs
+ * bottom-up (0: 24; the autotuner's tune_batch picks it per graph class).
  */
 enum bw_batch_mode { BW_BATCH_GRAPHS = 0, BW_BATCH_SOURCES = 1 };
 

@@ -40,3 +40,19 @@ def test_many_sources(ctx):
         want, _ = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, int(s))
         assert np.array_equal(got[k], want), k
     assert res.units == 40
+
+
+def test_push_pull_divisor_keeps_depths(ctx):
+    """The batched BFS's push/pull divisor (cfg chunk_size) changes only
+    which levels run bottom-up: depths are identical for every divisor."""
+    import torch
+    from belewitte_gb300 import batch
+    g = bw.DeviceGraph.generate("rmat", scale=14, edge_factor=16, seed=3, symmetrise=True)
+    srcs = [0, 5, 77, 1000, 4095]
+    ref = None
+    for d in (0, 2, 4, 24, 96, 100000):
+        levels, _ = batch.run_sources(ctx, g, srcs, bu_div=d)
+        got = levels.cpu()
+        if ref is None:
+            ref = got
+        assert torch.equal(got, ref), d
