@@ -29,6 +29,7 @@ The same JSON line carries:
   python bench.py --case pagerank:VARIANT:rmat22|er[:BLOCK:HUBS]   (small profiling case)
   python bench.py --case bfs:VARIANT:rmat22            (small profiling case)
   python bench.py --case bfsgraph:VARIANT:grid          (device loop; the cluster kernel)
+  python bench.py --case batch:graphs:COUNT             (the first COUNT batched graphs; k_batch)
   python bench.py --sweep      (every PageRank variant on R-MAT-22 and ER, every BFS variant
                                 on R-MAT-24 sym, the grid and BA)
 
@@ -507,6 +508,21 @@ def run_case(spec: str):
     algo, variant, graph, *shape = spec.split(":")
     block, hubs = (int(shape[0]), int(shape[1])) if len(shape) == 2 else (0, 0)
     ctx = bw.Context(0)
+    if algo == "batch":
+        # batch:graphs:COUNT -- the first COUNT graphs of the batched
+        # workload (BFS + 20 PageRank iterations each), one warm-up launch,
+        # then the profiled one
+        from belewitte_gb300 import batch
+        specs = batch.workload_a_specs(4096, seed=5)[:int(graph)]
+        gs = [bw.DeviceGraph.generate("rmat", scale=s["scale"], edge_factor=s["edge_factor"], seed=s["seed"])
+              for s in specs]
+        packed = batch.pack(gs)
+        del gs
+        for _ in range(2):
+            _, _, res = batch.run_graphs(ctx, packed, pr_iterations=20)
+        torch.cuda.synchronize()
+        print("case done", spec, f"{res.device_ms:.3f} ms, {packed.vertex_count} vertices, {packed.edge_count} edges")
+        return
     if graph == "er":
         g = bw.DeviceGraph.generate("er", n=4194304, m=67108864, seed=23, reps=63)
     elif graph == "rmat24s":
