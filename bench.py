@@ -282,7 +282,9 @@ class HostToDevice:
     """The e2e leg: a caller holding the CSR in pinned host memory copies it
     to preallocated device buffers every step and derives the edge-list /
     struct-edge-list arrays the variant reads on the device (as
-    DeviceGraph does), then calls bw_pagerank_run through the C ABI."""
+    DeviceGraph does), then calls bw_pagerank_run through the C ABI.  Pull
+    variants get the reverse CSR plus the forward offsets (for the
+    out-degrees)."""
 
     def __init__(self, host, variant, n, m, dev):
         import torch
@@ -293,6 +295,11 @@ class HostToDevice:
         self.st = "struct" in variant
         self.host = {k: torch.from_numpy(host[f"{side}_{k}"].view(np.int32)).pin_memory()
                      for k in ("vertices", "edges")}
+        if side == "rev":
+            # the forward offsets as well (4(N+1) bytes): the out-degrees are
+            # then their row lengths, one pass over N, instead of a histogram
+            # over the M source ids of the reverse CSR
+            self.host["out_offsets"] = torch.from_numpy(host["fwd_vertices"].view(np.int32)).pin_memory()
         self.dev = {k: torch.empty_like(v, device=f"cuda:{dev}") for k, v in self.host.items()}
         self.in_edges = torch.empty(max(m, 1), dtype=torch.int32, device=f"cuda:{dev}") if self.el else None
         self.struct = torch.empty(2 * max(m, 1), dtype=torch.int32, device=f"cuda:{dev}") if self.st else None
@@ -316,7 +323,7 @@ class HostToDevice:
         if self.side == "fwd":
             v = _abi.GraphView(self.n, self.m, off, adj, 0, 0, inn, 0, st, 0)
         else:
-            v = _abi.GraphView(self.n, self.m, 0, 0, off, adj, 0, inn, 0, st)
+            v = _abi.GraphView(self.n, self.m, self.dev["out_offsets"].data_ptr(), 0, off, adj, 0, inn, 0, st)
 
         class _View:
             vertex_count, edge_count, view = self.n, self.m, v
