@@ -30,7 +30,7 @@ constexpr uint32_t BATCH_HEAVY = 1024;    // rows above this are expanded by the
 constexpr uint32_t HEAVY_SLOTS = 256;
 constexpr uint32_t NO_UNIT = 0xffffffffu;
 constexpr float DAMPING = 0.85f;
-constexpr uint32_t BATCH_PR_LIGHT = 64;   // PageRank rows above this are summed by a whole warp
+constexpr uint32_t BATCH_PR_LIGHT = 256;  // PageRank rows above this are summed by a whole warp
 constexpr int BATCH_PR_UNROLL = 8;
 constexpr int BATCH_BFS_UNROLL = 4;
 constexpr uint32_t BATCH_BU_DIV = 24;     // default push/pull divisor: bottom-up above 1/24 of the unit
