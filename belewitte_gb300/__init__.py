@@ -117,6 +117,13 @@ class HostGraph:
                          int(symmetrise), what="bw_generate_rmat")
 
     @classmethod
+    def rmat_n(cls, n: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19,
+               c: float = 0.19, seed: int = 1, symmetrise: bool = False) -> "HostGraph":
+        """R-MAT over `n` vertices (any n >= 2; bw_generate_rmat_n)."""
+        return cls._make(library().bw_generate_rmat_n, n, edge_factor, a, b, c, seed,
+                         int(symmetrise), what="bw_generate_rmat_n")
+
+    @classmethod
     def erdos_renyi(cls, n: int, m: int, seed: int = 1, symmetrise: bool = False) -> "HostGraph":
         return cls._make(library().bw_generate_er, n, m, seed, int(symmetrise), what="bw_generate_er")
 
@@ -296,7 +303,8 @@ class DeviceGraph:
         torch = _torch()
         dev = torch.device("cuda", device)
         st = stream or torch.cuda.current_stream(dev)
-        kinds = {"rmat": (0, scale, edge_factor), "er": (1, n, m), "grid": (2, h, w), "ba": (3, n, m)}
+        kinds = {"rmat": (0, scale, edge_factor), "er": (1, n, m), "grid": (2, h, w), "ba": (3, n, m),
+                 "rmat_n": (4, n, edge_factor)}
         k, p0, p1 = kinds[kind]
         raw = _abi.DeviceGraphC()
         check(library().bw_generate_device(k, p0, p1, a, b, c, seed, int(symmetrise), C.byref(raw),

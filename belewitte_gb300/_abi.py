@@ -86,6 +86,8 @@ SIGNATURES = {
     "bw_graph_from_edges": (C.c_int, [C.c_uint64, C.c_uint64, u32p, u32p, C.c_int, C.POINTER(HostGraphC)]),
     "bw_generate_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                    C.c_uint64, C.c_int, C.POINTER(HostGraphC)]),
+    "bw_generate_rmat_n": (C.c_int, [C.c_uint64, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                     C.c_uint64, C.c_int, C.POINTER(HostGraphC)]),
     "bw_generate_er": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int, C.POINTER(HostGraphC)]),
     "bw_generate_grid": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(HostGraphC)]),
     "bw_generate_ba": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(HostGraphC)]),

@@ -117,8 +117,22 @@ def tune(ctx, g, algorithm: str, variants=None, *, root: int = 0, repeats: int =
     return out
 
 
+# A tuned entry is used for graphs whose shape class is at most this far
+# (sum of the log2 differences of vertices, average degree and skew) from
+# the class it was tuned on; farther graphs keep the library default.
+MAX_CLASS_DISTANCE = 2
+
+
+def class_distance(a: str, b: str) -> int:
+    """Sum of the differences of two shape classes' log2 fields."""
+    x = [int(t[1:]) for t in a.split("-")]
+    y = [int(t[1:]) for t in b.split("-")]
+    return sum(abs(p - q) for p, q in zip(x, y))
+
+
 def lookup(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
-    """The tuned configuration for the nearest cached shape class (or {})."""
+    """The tuned configuration for the nearest cached shape class within
+    MAX_CLASS_DISTANCE (or {}: the library default)."""
     if not cache.exists():
         return {}
     entries = json.loads(cache.read_text()).get(algorithm, {}).get(name, {})
@@ -127,12 +141,9 @@ def lookup(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
     cls = shape_class(g)
     if cls in entries:
         return dict(entries[cls]["config"])
-
-    def dist(other: str) -> int:
-        a = [int(x[1:]) for x in cls.split("-")]
-        b = [int(x[1:]) for x in other.split("-")]
-        return sum(abs(x - y) for x, y in zip(a, b))
-    near = min(entries, key=dist)
+    near = min(entries, key=lambda other: class_distance(cls, other))
+    if class_distance(cls, near) > MAX_CLASS_DISTANCE:
+        return {}
     return dict(entries[near]["config"])
 
 
@@ -170,8 +181,8 @@ def batch_key(mode: str, g=None) -> str:
 
 
 def lookup_batch(mode: str, g=None, cache: Path = CACHE) -> int:
-    """The tuned divisor for this mode (and the nearest shape class of `g`
-    for sources), or 0 (the library default)."""
+    """The tuned divisor for this mode (and, for sources, the nearest shape
+    class of `g` within MAX_CLASS_DISTANCE), or 0 (the library default)."""
     if not cache.exists():
         return 0
     entries = json.loads(cache.read_text()).get("batch", {})
@@ -183,9 +194,8 @@ def lookup_batch(mode: str, g=None, cache: Path = CACHE) -> int:
     cands = [k for k in entries if k.startswith("sources/")]
     if not cands:
         return 0
-    cls = [int(x[1:]) for x in shape_class(g).split("-")]
-
-    def dist(k: str) -> int:
-        other = [int(x[1:]) for x in k.split("/", 1)[1].split("-")]
-        return sum(abs(x - y) for x, y in zip(cls, other))
-    return int(entries[min(cands, key=dist)]["bu_div"])
+    cls = shape_class(g)
+    near = min(cands, key=lambda k: class_distance(cls, k.split("/", 1)[1]))
+    if class_distance(cls, near.split("/", 1)[1]) > MAX_CLASS_DISTANCE:
+        return 0
+    return int(entries[near]["bu_div"])

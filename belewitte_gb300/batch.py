@@ -113,12 +113,15 @@ def run_sources(ctx, g: DeviceGraph, sources, levels=None, grid: int = 0, stream
     return levels, res
 
 
-def workload_a_specs(count: int = 4096, seed: int = 5, min_scale: float = 10.0, max_scale: float = 17.6):
-    """Seeded R-MAT graphs with log-uniform vertex counts (powers of two,
-    2^10 .. 2^17) and edge factors 8-32."""
+def workload_a_specs(count: int = 4096, seed: int = 5, min_vertices: int = 1000, max_vertices: int = 200000):
+    """Seeded R-MAT graphs with vertex counts drawn log-uniformly from
+    [min_vertices, max_vertices] and edge factors 8-32 (generated with
+    DeviceGraph.generate("rmat_n", n=..., edge_factor=...))."""
     rng = np.random.default_rng(seed)
+    lo, hi = np.log(min_vertices), np.log(max_vertices)
     out = []
-    for i in range(count):
-        scale = int(round(rng.uniform(min_scale, max_scale)))
-        out.append(dict(scale=scale, edge_factor=int(rng.integers(8, 33)), seed=int(rng.integers(1, 2 ** 31))))
+    for _ in range(count):
+        n = int(round(float(np.exp(rng.uniform(lo, hi)))))
+        out.append(dict(n=min(max(n, min_vertices), max_vertices), edge_factor=int(rng.integers(8, 33)),
+                        seed=int(rng.integers(1, 2 ** 31))))
     return out

@@ -32,7 +32,8 @@ __global__ void k_gen_keys(GenParams p, uint64_t count, uint64_t *keys)
           case 0: bwgen::rmat_edge(p.rmat, p.seed, i, s, d); break;
           case 1: bwgen::er_edge(p.p0, p.seed, i, s, d); break;
           case 2: bwgen::grid_edge(p.p0, p.p1, i, s, d); break;
-          default: bwgen::ba_edge(p.p1, p.seed, i, s, d); break;
+          case 3: bwgen::ba_edge(p.p1, p.seed, i, s, d); break;
+          default: bwgen::rmat_edge_n(p.rmat, p.p0, p.seed, i, s, d); break;
         }
         const bool drop = p.drop_self && s == d;
         if (p.symmetrise) {
@@ -101,7 +102,7 @@ void bw_device_graph_free(bw_device_graph *g)
 int bw_generate_device(int kind, uint64_t p0, uint64_t p1, double a, double b, double c, uint64_t seed,
                        int symmetrise, bw_device_graph *out, void *stream)
 {
-    if (!out || kind < 0 || kind > 3) return BW_ERR_INVALID_ARGUMENT;
+    if (!out || kind < 0 || kind > 4) return BW_ERR_INVALID_ARGUMENT;
     *out = bw_device_graph{};
     cudaStream_t s = as_stream(stream);
     GenParams gp{};
@@ -132,10 +133,18 @@ int bw_generate_device(int kind, uint64_t p0, uint64_t p1, double a, double b, d
         gp.symmetrise = 1;
         dedupe = false;
         break;
-      default:
+      case 3:
         if (p0 < 2 || p0 > 0xffffffffULL || p1 == 0) return BW_ERR_INVALID_ARGUMENT;
         n = p0; count = p0 * p1;
         gp.symmetrise = 1;
+        break;
+      default:
+        if (p0 < 2 || p0 > 0x80000000ULL || p1 == 0 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0)
+            return BW_ERR_INVALID_ARGUMENT;
+        n = p0;
+        count = n * p1;
+        gp.rmat = bwgen::rmat_params(static_cast<uint32_t>(bits_for(n)), a, b, c);
+        gp.symmetrise = symmetrise != 0;
         break;
     }
     gp.vb = bits_for(n);

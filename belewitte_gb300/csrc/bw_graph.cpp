@@ -253,6 +253,22 @@ int bw_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
     return finish_graph(keys, n, bits_for(n), true, symmetrise != 0, out);
 }
 
+int bw_generate_rmat_n(uint64_t n, uint32_t edge_factor, double a, double b,
+                       double c, uint64_t seed, int symmetrise, bw_host_graph *out)
+{
+    if (!out || n < 2 || n > 0x80000000ULL || edge_factor == 0) return BW_ERR_INVALID_ARGUMENT;
+    if (a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return BW_ERR_INVALID_ARGUMENT;
+    const int vb = bits_for(n);
+    const bwgen::RmatParams p = bwgen::rmat_params(static_cast<uint32_t>(vb), a, b, c);
+    const int flags = BW_BUILD_DROP_SELF_LOOPS | BW_BUILD_DEDUPE |
+                      (symmetrise ? BW_BUILD_SYMMETRISE : 0);
+    std::vector<uint64_t> keys;
+    int rc = generate_keys(n * edge_factor, n, flags,
+        [&](uint64_t e, uint64_t& s, uint64_t& d) { bwgen::rmat_edge_n(p, n, seed, e, s, d); }, keys);
+    if (rc) return rc;
+    return finish_graph(keys, n, vb, true, symmetrise != 0, out);
+}
+
 int bw_generate_er(uint64_t n, uint64_t m, uint64_t seed, int symmetrise,
                    bw_host_graph *out)
 {

@@ -61,6 +61,16 @@ BW_HD void rmat_edge(const RmatParams &p, uint64_t seed, uint64_t e, uint64_t &s
     d = dv;
 }
 
+// R-MAT over n vertices, n not necessarily a power of two (p.scale =
+// ceil(log2 n)): the power-of-two generator's edge e with both endpoints
+// scaled by n / 2^scale (multiply-shift), so the low ids keep the hubs.
+BW_HD void rmat_edge_n(const RmatParams &p, uint64_t n, uint64_t seed, uint64_t e, uint64_t &s, uint64_t &d)
+{
+    rmat_edge(p, seed, e, s, d);
+    s = (s * n) >> p.scale;
+    d = (d * n) >> p.scale;
+}
+
 BW_HD void er_edge(uint64_t n, uint64_t seed, uint64_t e, uint64_t &s, uint64_t &d)
 {
     s = bounded(hash3(seed, e, 0), n);

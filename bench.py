@@ -252,14 +252,15 @@ def batched(ctx, dev, graphs: int):
     out = {}
     t0 = time.time()
     specs = batch.workload_a_specs(graphs, seed=5)
-    gs = [bw.DeviceGraph.generate("rmat", scale=s["scale"], edge_factor=s["edge_factor"], seed=s["seed"],
+    gs = [bw.DeviceGraph.generate("rmat_n", n=s["n"], edge_factor=s["edge_factor"], seed=s["seed"],
                                   device=dev) for s in specs]
     packed = batch.pack(gs, device=dev)
     del gs
     gen_s = time.time() - t0
     batch.run_graphs(ctx, packed, pr_iterations=20)                     # warm-up
     _, _, res = batch.run_graphs(ctx, packed, pr_iterations=20)
-    out["graphs"] = {"workload": f"{graphs} R-MAT graphs, 2^10..2^18 vertices, edge factor 8-32; "
+    out["graphs"] = {"workload": f"{graphs} R-MAT graphs, vertex counts log-uniform in 1,000..200,000, "
+                                 "edge factor 8-32; "
                                  "BFS from each max-degree vertex + 20 PageRank iterations, one persistent launch",
                      "vertices": packed.vertex_count, "edges": packed.edge_count, "ms": round(res.device_ms, 3),
                      "gteps": round((res.traversed_edges + 20 * packed.edge_count) / (res.device_ms * 1e-3) / 1e9, 2),
@@ -521,7 +522,7 @@ def run_case(spec: str):
         # then the profiled one
         from belewitte_gb300 import batch
         specs = batch.workload_a_specs(4096, seed=5)[:int(graph)]
-        gs = [bw.DeviceGraph.generate("rmat", scale=s["scale"], edge_factor=s["edge_factor"], seed=s["seed"])
+        gs = [bw.DeviceGraph.generate("rmat_n", n=s["n"], edge_factor=s["edge_factor"], seed=s["seed"])
               for s in specs]
         packed = batch.pack(gs)
         del gs

@@ -129,6 +129,8 @@ int bw_graph_from_edges(uint64_t vertex_count, uint64_t count,
  * the same graph on every machine and thread count).  All drop self-loops and
  * duplicate edges.
  *   R-MAT(a,b,c,d=1-a-b-c), 2^scale vertices, edge_factor*2^scale samples.
+ *   R-MAT over n vertices (any n >= 2): edge_factor*n samples of the R-MAT
+ *     of scale ceil(log2 n), both endpoints scaled by n / 2^scale.
  *   Erdos-Renyi G(n,m): m uniform (u,v) samples.
  *   2-D 4-neighbour grid h x w, both directions (evolve/gen-graph.cpp:96-123).
  *   Barabasi-Albert: n vertices, m attachments each, both directions.
@@ -136,6 +138,9 @@ int bw_graph_from_edges(uint64_t vertex_count, uint64_t count,
 int bw_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
                      double c, uint64_t seed, int symmetrise,
                      bw_host_graph *out);
+int bw_generate_rmat_n(uint64_t n, uint32_t edge_factor, double a, double b,
+                       double c, uint64_t seed, int symmetrise,
+                       bw_host_graph *out);
 int bw_generate_er(uint64_t n, uint64_t m, uint64_t seed, int symmetrise,
                    bw_host_graph *out);
 int bw_generate_grid(uint32_t h, uint32_t w, bw_host_graph *out);
@@ -164,7 +169,9 @@ typedef struct bw_device_graph {
  * kind: 0 R-MAT(p0 = scale, p1 = edge factor, a, b, c),
  *       1 Erdos-Renyi(p0 = n, p1 = m),
  *       2 grid(p0 = h, p1 = w),
- *       3 Barabasi-Albert(p0 = n, p1 = m).
+ *       3 Barabasi-Albert(p0 = n, p1 = m),
+ *       4 R-MAT over any vertex count (p0 = n, p1 = edge factor, a, b, c;
+ *         as bw_generate_rmat_n).
  * Sorting uses CUB radix sort (input preparation, not a hot path).
  */
 int bw_generate_device(int kind, uint64_t p0, uint64_t p1, double a, double b,
@@ -603,10 +610,17 @@ int bw_batch_run(bw_context *ctx, const bw_graph_view *g, int mode,
  * device array of about 9.2 MB that every GPU loading the library holds
  * until exit.  Limits: at most 1,048,576 vertices and 16,777,216 edges;
  * larger graphs return BW_ERR_TOO_LARGE.  The first call on a device looks up
- * that array's device address (with the device current); make that first
- * call before any stream capture.  Every call shares the one array and
- * re-initialises it: calls that overlap on the GPU (other streams, other
- * threads) race and must not be issued.  Depths are identical to
+ * that array's device address (with the device current) and keeps it for
+ * the life of the process.  With lazy module loading (the CUDA 13 default)
+ * that first call is also when the array is reserved on the device, so make
+ * one warm-up call per device at start-up (a one-vertex graph will do),
+ * before reserving the rest of the HBM budget and before any stream capture.
+ * Do not call it again on a device after cudaDeviceReset: the kept address
+ * belongs to the old context.  Each call reads every level's frontier size
+ * back to the host, synchronising `stream` once per level, so it returns with
+ * the BFS complete.  Every call shares the one array and re-initialises it:
+ * calls that overlap on the GPU (other streams, other threads) race and must
+ * not be issued.  Depths are identical to
  * bw_bfs_run(..., "frontier-push", ...); *level_count gets the levels run.
  */
 int bw_bfs_run_noalloc(const bw_graph_view *g, uint32_t root, int32_t *levels,

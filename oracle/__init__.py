@@ -7,6 +7,7 @@ baseline, never as part of the product path.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -18,6 +19,12 @@ PR_DIV, PR_NODIV = 0, 1
 INF = 2147483647
 
 _lib = None
+
+
+class OrGraph(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("m", C.c_uint64),
+                ("fwd_off", C.POINTER(C.c_uint32)), ("fwd_edges", C.POINTER(C.c_uint32)),
+                ("rev_off", C.POINTER(C.c_uint32)), ("rev_edges", C.POINTER(C.c_uint32))]
 
 
 def build(force: bool = False) -> Path:
@@ -47,6 +54,11 @@ def lib() -> C.CDLL:
         l.or_pagerank_f64.argtypes = [C.c_int, C.c_uint64, u32p, u32p, u32p, C.c_uint32, f64p]
         l.or_pagerank_parallel.restype = None
         l.or_pagerank_parallel.argtypes = [C.c_uint64, u32p, u32p, u32p, C.c_uint32, f32p, C.c_int]
+        l.or_generate_rmat.restype = C.c_int
+        l.or_generate_rmat.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                       C.c_int, C.POINTER(OrGraph)]
+        l.or_graph_free.restype = None
+        l.or_graph_free.argtypes = [C.POINTER(OrGraph)]
         l.or_format_rank.restype = C.c_int
         l.or_format_rank.argtypes = [C.c_float, C.c_char_p, C.c_int]
         _lib = l
@@ -123,17 +135,45 @@ def pagerank_parallel(n, rev_off, rev_edges, iterations, deg=None, threads=0):
     return pr
 
 
+def generate_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetrise=False) -> dict:
+    """The library's seeded R-MAT graph, made here without the library:
+    {"fwd_vertices", "fwd_edges", "rev_vertices", "rev_edges"} (uint32)."""
+    g = OrGraph()
+    if lib().or_generate_rmat(scale, edge_factor, a, b, c, seed, int(symmetrise), C.byref(g)) != 0:
+        raise MemoryError("or_generate_rmat failed")
+    try:
+        n, m = int(g.n), int(g.m)
+
+        def grab(ptr, count):
+            return np.ctypeslib.as_array(ptr, shape=(count,)).copy() if count else np.zeros(0, np.uint32)
+        out = {"fwd_vertices": grab(g.fwd_off, n + 1), "fwd_edges": grab(g.fwd_edges, m)}
+        if symmetrise:
+            out["rev_vertices"], out["rev_edges"] = out["fwd_vertices"], out["fwd_edges"]
+        else:
+            out["rev_vertices"], out["rev_edges"] = grab(g.rev_off, n + 1), grab(g.rev_edges, m)
+        return out
+    finally:
+        lib().or_graph_free(C.byref(g))
+
+
 def format_rank(value: float) -> str:
     buf = C.create_string_buffer(64)
     lib().or_format_rank(float(value), buf, 64)
     return buf.value.decode()
 
 
-def build_ref(reference_root: str = "/root/reference", force: bool = False) -> list[Path]:
+def build_ref(reference_root: str | None = None, force: bool = False) -> list[Path]:
     """Compile the reference's CUDA kernels, unmodified, into cubins under
     oracle/_ref/ (the parity pin run by oracle/ref_runner.py).  Only runs
     where the reference tree exists; elsewhere the prebuilt cubins are used.
+
+    The tree is `reference_root`, else the BELEWITTE_REFERENCE environment
+    variable; with neither, nothing is compiled.
     """
+    reference_root = reference_root or os.environ.get("BELEWITTE_REFERENCE", "")
+    if not reference_root:
+        out_dir = HERE / "_ref"
+        return sorted(out_dir.glob("*.cubin")) if out_dir.exists() else []
     root = Path(reference_root)
     out_dir = HERE / "_ref"
     units = {"ref_bfs": "ref_bfs_unity.cu", "ref_pagerank": "ref_pagerank_unity.cu",

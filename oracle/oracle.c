@@ -277,3 +277,170 @@ int or_format_rank(float value, char *buf, int len)
 {
     return snprintf(buf, (size_t) len, "%.7g", (double) value);
 }
+
+/*
+ * Seeded R-MAT graph, built without the product library, so that the
+ * reference arm of the benchmark and the CPU baselines can make the very
+ * graph the GPU runs on.  It restates the library's own counter-based
+ * generator (not a reference algorithm; the reference's generator is
+ * evolve/gen-graph.cpp, which has no R-MAT): edge e draws scale quadrant
+ * choices, two per 64-bit hash of (seed, e, level / 2), most significant
+ * bit first, with the cumulative probabilities a, a+b, a+b+c scaled to 2^32.
+ * Self-loops and duplicates are dropped; rows of the forward and reverse
+ * CSR are sorted.  The CSR arrays are malloc'd (or_graph_free).
+ */
+static uint64_t or_mix64(uint64_t z)
+{
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+static uint64_t or_hash3(uint64_t seed, uint64_t a, uint64_t b)
+{
+    return or_mix64(or_mix64(seed ^ or_mix64(a)) ^ (b * 0xd1b54a32d192ed03ULL));
+}
+
+static int or_cmp_u32(const void *x, const void *y)
+{
+    const uint32_t a = *(const uint32_t *) x, b = *(const uint32_t *) y;
+    return (a > b) - (a < b);
+}
+
+/* Counting sort of (src[i], dst[i]) pairs, i < count, into rows of n
+ * (pairs with src == UINT32_MAX skipped); every row sorted and de-duplicated
+ * when `unique`.  Deterministic for any thread count: threads own contiguous
+ * input ranges and write each row's entries in input order. */
+static int or_pairs_to_csr(uint64_t n, uint64_t count, const uint32_t *src, const uint32_t *dst,
+                           int unique, uint32_t **off_out, uint32_t **edges_out, uint64_t *m_out)
+{
+    int T = 1;
+#ifdef _OPENMP
+    T = omp_get_max_threads();
+#endif
+    uint64_t *cnt = (uint64_t *) calloc((size_t) T * (n + 1), sizeof(uint64_t));
+    uint32_t *buf = (uint32_t *) malloc((count ? count : 1) * sizeof(uint32_t));
+    uint64_t *start = (uint64_t *) malloc((n + 1) * sizeof(uint64_t));
+    uint32_t *len = (uint32_t *) malloc((n ? n : 1) * sizeof(uint32_t));
+    if (!cnt || !buf || !start || !len) { free(cnt); free(buf); free(start); free(len); return -1; }
+#pragma omp parallel num_threads(T)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        const uint64_t lo = count * (uint64_t) t / (uint64_t) T, hi = count * (uint64_t) (t + 1) / (uint64_t) T;
+        uint64_t *c = cnt + (size_t) t * (n + 1);
+        for (uint64_t i = lo; i < hi; i++)
+            if (src[i] != UINT32_MAX) c[src[i]]++;
+#pragma omp barrier
+#pragma omp single
+        {
+            uint64_t sum = 0;
+            for (uint64_t r = 0; r < n; r++) {
+                start[r] = sum;
+                for (int tt = 0; tt < T; tt++) {
+                    const uint64_t k = cnt[(size_t) tt * (n + 1) + r];
+                    cnt[(size_t) tt * (n + 1) + r] = sum;
+                    sum += k;
+                }
+            }
+            start[n] = sum;
+        }
+        for (uint64_t i = lo; i < hi; i++)
+            if (src[i] != UINT32_MAX) buf[c[src[i]]++] = dst[i];
+    }
+    free(cnt);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t r = 0; r < (int64_t) n; r++) {
+        uint32_t *row = buf + start[r];
+        const uint64_t k = start[r + 1] - start[r];
+        if (k > 1) qsort(row, k, sizeof(uint32_t), or_cmp_u32);
+        uint64_t w = k;
+        if (unique && k > 1) {
+            w = 1;
+            for (uint64_t i = 1; i < k; i++)
+                if (row[i] != row[w - 1]) row[w++] = row[i];
+        }
+        len[r] = (uint32_t) w;
+    }
+    uint32_t *off = (uint32_t *) malloc((n + 1) * sizeof(uint32_t));
+    uint64_t m = 0;
+    for (uint64_t r = 0; r < n; r++) m += len[r];
+    uint32_t *edges = (uint32_t *) malloc((m ? m : 1) * sizeof(uint32_t));
+    if (!off || !edges || m > 0xffffffffULL) { free(off); free(edges); free(buf); free(start); free(len); return -1; }
+    uint64_t acc = 0;
+    for (uint64_t r = 0; r < n; r++) { off[r] = (uint32_t) acc; acc += len[r]; }
+    off[n] = (uint32_t) acc;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t r = 0; r < (int64_t) n; r++)
+        memcpy(edges + off[r], buf + start[r], (size_t) len[r] * sizeof(uint32_t));
+    free(buf); free(start); free(len);
+    *off_out = off; *edges_out = edges; *m_out = m;
+    return 0;
+}
+
+int or_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                     int symmetrise, or_graph *out)
+{
+    memset(out, 0, sizeof *out);
+    if (scale < 1 || scale > 31 || edge_factor == 0) return -1;
+    const uint64_t n = (uint64_t) 1 << scale, count = n * edge_factor, total = count * (symmetrise ? 2 : 1);
+    const double two32 = 4294967296.0;
+    const uint64_t ta = (uint64_t) (a * two32), tab = (uint64_t) ((a + b) * two32),
+                   tabc = (uint64_t) ((a + b + c) * two32);
+    uint32_t *src = (uint32_t *) malloc(total * sizeof(uint32_t));
+    uint32_t *dst = (uint32_t *) malloc(total * sizeof(uint32_t));
+    if (!src || !dst) { free(src); free(dst); return -1; }
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (int64_t) count; e++) {
+        uint64_t sv = 0, dv = 0, h = 0;
+        for (uint32_t l = 0; l < scale; l++) {
+            uint64_t r;
+            if ((l & 1) == 0) { h = or_hash3(seed, (uint64_t) e, l >> 1); r = h & 0xffffffffULL; }
+            else r = h >> 32;
+            const uint64_t sb = r >= tab, db = (r >= ta && r < tab) || r >= tabc;
+            sv = (sv << 1) | sb;
+            dv = (dv << 1) | db;
+        }
+        const int loop = sv == dv;
+        if (symmetrise) {
+            src[2 * e] = loop ? UINT32_MAX : (uint32_t) sv;  dst[2 * e] = (uint32_t) dv;
+            src[2 * e + 1] = loop ? UINT32_MAX : (uint32_t) dv;  dst[2 * e + 1] = (uint32_t) sv;
+        } else {
+            src[e] = loop ? UINT32_MAX : (uint32_t) sv;  dst[e] = (uint32_t) dv;
+        }
+    }
+    int rc = or_pairs_to_csr(n, total, src, dst, 1, &out->fwd_off, &out->fwd_edges, &out->m);
+    free(src); free(dst);
+    if (rc) return rc;
+    out->n = n;
+    if (symmetrise) {
+        out->rev_off = out->fwd_off;
+        out->rev_edges = out->fwd_edges;
+        return 0;
+    }
+    /* reverse CSR: the forward edges counted by destination, in source
+     * order (so each reverse row comes out sorted) */
+    const uint64_t m = out->m;
+    uint32_t *rs = (uint32_t *) malloc((m ? m : 1) * sizeof(uint32_t));
+    if (!rs) { or_graph_free(out); return -1; }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t u = 0; u < (int64_t) n; u++)
+        for (uint32_t k = out->fwd_off[u]; k < out->fwd_off[u + 1]; k++) rs[k] = (uint32_t) u;
+    uint64_t m2 = 0;
+    rc = or_pairs_to_csr(n, m, out->fwd_edges, rs, 0, &out->rev_off, &out->rev_edges, &m2);
+    free(rs);
+    if (rc || m2 != m) { or_graph_free(out); return -1; }
+    return 0;
+}
+
+void or_graph_free(or_graph *g)
+{
+    if (g->rev_off != g->fwd_off) free(g->rev_off);
+    if (g->rev_edges != g->fwd_edges) free(g->rev_edges);
+    free(g->fwd_off);
+    free(g->fwd_edges);
+    memset(g, 0, sizeof *g);
+}

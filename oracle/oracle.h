@@ -28,6 +28,16 @@ void or_pagerank_parallel(uint64_t n, const uint32_t *rev_off,
                           uint32_t iterations, float *pr, int threads);
 int or_format_rank(float value, char *buf, int len);
 
+/* A seeded R-MAT graph (forward + reverse CSR, malloc'd), made without the
+ * product library; identical to its bw_generate_rmat graph. */
+typedef struct {
+    uint64_t n, m;
+    uint32_t *fwd_off, *fwd_edges, *rev_off, *rev_edges;
+} or_graph;
+int or_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                     int symmetrise, or_graph *out);
+void or_graph_free(or_graph *g);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,8 +41,13 @@ def test_lookup_batch_sources_nearest_shape_class(tmp_path):
     assert key_big.startswith("sources/v12-")
     cache.write_text(json.dumps({"batch": {key_big: {"bu_div": 1024, "ms": 1.0}}}))
     assert autotune.lookup_batch("sources", g_big, cache=cache) == 1024
-    # no entry for this class: the nearest cached class
-    assert autotune.lookup_batch("sources", g_small, cache=cache) == 1024
+    # no entry for this class: the nearest cached class, when it is close
+    g_near = _Graph(1 << 13, 16 << 13, 8000)
+    assert autotune.batch_key("sources", g_near) != key_big
+    assert autotune.lookup_batch("sources", g_near, cache=cache) == 1024
+    # a graph far from every cached class keeps the library default
+    assert autotune.class_distance(key_big.split("/")[1], autotune.shape_class(g_small)) > autotune.MAX_CLASS_DISTANCE
+    assert autotune.lookup_batch("sources", g_small, cache=cache) == 0
     # other modes and missing caches fall back to the library default (0)
     assert autotune.lookup_batch("graphs", cache=cache) == 0
     assert autotune.lookup_batch("sources", g_big, cache=tmp_path / "none.json") == 0

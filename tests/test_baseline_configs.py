@@ -1,0 +1,177 @@
+"""Parity at the benchmark configurations' own sizes, not only on the small
+parity graphs.
+
+  * Configuration 1: R-MAT scale 16, edge factor 16 (seed 16), BFS from the
+    highest out-degree vertex with every variant, PageRank with every
+    variant for 30 iterations -- ours and the reference's own kernels, both
+    against the oracle.
+  * The headline PageRank workload: R-MAT scale 22, edge factor 16 (seed
+    22), 30 iterations.  The pull variants are compared bit for bit with the
+    oracle's OpenMP vertex-pull and with the reference's own vertex-pull
+    kernel run on the same graph, and with the FP64 oracle within 1e-4.
+  * Configuration 2's second graph, ER(4,194,304, 67,108,864), the same way.
+  * Configuration 3's BFS graphs (R-MAT scale 24 symmetrised, the 4096 x
+    4096 grid, BA(8M, 8)): seeded sources from the giant component, every
+    fixed candidate variant and the learned switch against the oracle.
+
+Tolerances: BFS depths bit-exact; PageRank pull variants bit-exact (the
+reference's sequential row order); float-atomic variants (edge lists, push,
+warp pull) within 1e-5 of the oracle and 1e-4 of FP64.
+"""
+import numpy as np
+import pytest
+
+import belewitte_gb300 as bw
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+BITEXACT = {"vertex-pull", "vertex-pull-nodiv", "pull-segmented"}
+REL_REF, REL_F64 = 1e-5, 1e-4
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float((np.abs(a - b) / np.abs(b)).max())
+
+
+def _ref_kernels():
+    from oracle import ref_runner
+    return ref_runner.ReferenceKernels() if ref_runner.cubins_present() else None
+
+
+# --------------------------------------------------------------- config 1
+@pytest.fixture(scope="module")
+def config1():
+    h = bw.HostGraph.rmat(16, 16, seed=16)
+    root = h.max_out_degree_vertex()
+    lv, cnt = oracle.bfs(h.vertex_count, h.fwd_vertices, h.fwd_edges, root)
+    return h, bw.DeviceGraph(h), root, lv, cnt
+
+
+def test_config1_bfs_every_variant(ctx, config1):
+    from belewitte_gb300 import learn
+    h, g, root, lv, cnt = config1
+    for name in bw.bfs_variant_names():
+        for loop in ("host", "graph"):
+            run = bw.bfs(ctx, g, name, root, loop=loop)
+            assert np.array_equal(run.levels.cpu().numpy(), lv), (name, loop)
+            assert run.level_count == len(cnt), (name, loop)
+    run = learn.run_learned(ctx, g, learn.load_predictor(), root, loop="graph", stats=False)
+    assert np.array_equal(run.levels.cpu().numpy(), lv)
+
+
+def test_config1_pagerank_every_variant(ctx, config1):
+    h, g, _, _, _ = config1
+    n = h.vertex_count
+    div, _ = oracle.pagerank(oracle.PR_DIV, n, h.rev_vertices, h.rev_edges, 30)
+    nodiv, _ = oracle.pagerank(oracle.PR_NODIV, n, h.rev_vertices, h.rev_edges, 30)
+    d64 = oracle.pagerank_f64(oracle.PR_DIV, n, h.rev_vertices, h.rev_edges, 30)
+    n64 = oracle.pagerank_f64(oracle.PR_NODIV, n, h.rev_vertices, h.rev_edges, 30)
+    for name in bw.pagerank_variant_names():
+        for loop in ("host", "graph"):
+            got = bw.pagerank(ctx, g, name, 30, loop=loop).ranks.cpu().numpy()
+            ref, r64 = (nodiv, n64) if "nodiv" in name else (div, d64)
+            if name in BITEXACT:
+                assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (name, loop)
+            else:
+                assert _rel(got, ref) <= REL_REF, (name, loop, _rel(got, ref))
+            assert _rel(got, r64) <= REL_F64, (name, loop)
+
+
+def test_config1_reference_kernels(config1):
+    """The reference's own 32 BFS and 10 PageRank kernels on configuration 1
+    agree with the oracle (pinning the oracle at this size)."""
+    from oracle import ref_runner
+    ref = _ref_kernels()
+    if ref is None:
+        pytest.skip("reference cubins not present (built from the reference tree)")
+    h, _, root, lv, cnt = config1
+    dg = ref.upload_graph(h.vertex_count, h.fwd_vertices, h.fwd_edges, h.rev_vertices, h.rev_edges)
+    for name in ref_runner.bfs_variant_names():
+        rl, rc = ref.bfs(dg, name, root)
+        assert np.array_equal(rl, lv), name
+        assert np.array_equal(rc, cnt), name
+    n = h.vertex_count
+    for name in ref_runner.PR_VARIANTS:
+        sem = oracle.PR_NODIV if "nodiv" in name else oracle.PR_DIV
+        want, _ = oracle.pagerank(sem, n, h.rev_vertices, h.rev_edges, 30)
+        got, _ = ref.pagerank(dg, name, 30)
+        if name in ("vertex-pull", "vertex-pull-nodiv"):
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), name
+        else:
+            assert _rel(got, want) <= REL_REF, (name, _rel(got, want))
+
+
+# ------------------------------------------------- config 2 (full sizes)
+def _pagerank_full_size(ctx, kind, kw):
+    import torch
+    g = bw.DeviceGraph.generate(kind, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR, **kw)
+    host = g.to_host_arrays()
+    n = g.vertex_count
+    deg = np.diff(host["fwd_vertices"].astype(np.int64)).astype(np.uint32)
+    want = oracle.pagerank_parallel(n, host["rev_vertices"], host["rev_edges"], 30, deg=deg)
+    want_nd, _ = oracle.pagerank(oracle.PR_NODIV, n, host["rev_vertices"], host["rev_edges"], 30, deg=deg)
+    r64 = oracle.pagerank_f64(oracle.PR_DIV, n, host["rev_vertices"], host["rev_edges"], 30, deg=deg)
+    ranks = torch.empty(n, dtype=torch.float32, device="cuda")
+    for name in ("pull-segmented", "vertex-pull"):
+        for loop in ("host", "graph"):
+            got = bw.pagerank(ctx, g, name, 30, ranks=ranks, loop=loop).ranks.cpu().numpy()
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (kind, name, loop)
+    got = bw.pagerank(ctx, g, "vertex-pull-nodiv", 30, ranks=ranks).ranks.cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want_nd.view(np.uint32)), kind
+    for name in ("rev-edge-list", "vertex-push", "vertex-pull-warp"):
+        got = bw.pagerank(ctx, g, name, 30, ranks=ranks).ranks.cpu().numpy()
+        assert _rel(got, r64) <= REL_F64, (kind, name)
+    assert _rel(want, r64) <= REL_F64
+    ref = _ref_kernels()
+    if ref is not None:
+        del ranks
+        dg = ref.upload_graph(n, host["fwd_vertices"], host["fwd_edges"], host["rev_vertices"], host["rev_edges"])
+        got, _ = ref.pagerank(dg, "vertex-pull", 30)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), kind
+        del dg
+    del g
+    torch.cuda.empty_cache()
+
+
+def test_headline_pagerank_rmat22(ctx):
+    _pagerank_full_size(ctx, "rmat", dict(scale=22, edge_factor=16, seed=22))
+
+
+def test_config2_pagerank_er(ctx):
+    _pagerank_full_size(ctx, "er", dict(n=4194304, m=67108864, seed=23))
+
+
+# ------------------------------------------------- config 3 (full sizes)
+@pytest.mark.parametrize("kind,kw", [
+    ("rmat", dict(scale=24, edge_factor=16, seed=24, symmetrise=True)),
+    ("grid", dict(h=4096, w=4096)),
+    ("ba", dict(n=8388608, m=8, seed=8)),
+])
+def test_config3_bfs_sources(ctx, kind, kw):
+    """Two seeded sources of the giant component per graph (the bench runs
+    sixteen): the fixed candidates and the learned switch, depths against the
+    oracle's queue BFS."""
+    import torch
+    from belewitte_gb300 import learn
+    g = bw.DeviceGraph.generate(kind, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR, **kw)
+    host = g.to_host_arrays()
+    n = g.vertex_count
+    hub = int(np.argmax(np.diff(host["fwd_vertices"].astype(np.int64))))
+    reach, _ = oracle.bfs(n, host["fwd_vertices"], host["fwd_edges"], hub)
+    comp = np.flatnonzero(reach != oracle.INF)
+    pred = learn.load_predictor()
+    for r in np.random.default_rng(3).choice(comp, 2, replace=False):
+        want, cnt = oracle.bfs(n, host["fwd_vertices"], host["fwd_edges"], int(r))
+        for name in ("frontier-push", "frontier-pull", "edge-list-bulk", "vertex-pull-warp-bulk"):
+            if kind == "grid" and not name.startswith("frontier"):
+                continue                      # 8190 levels of O(M) work each
+            run = bw.bfs(ctx, g, name, int(r), loop="graph")
+            assert np.array_equal(run.levels.cpu().numpy(), want), (kind, name, r)
+            assert run.level_count == len(cnt)
+        run = learn.run_learned(ctx, g, pred, int(r), loop="graph", stats=False)
+        assert np.array_equal(run.levels.cpu().numpy(), want), (kind, "learned", r)
+    del g
+    torch.cuda.empty_cache()

@@ -10,8 +10,8 @@ pytestmark = pytest.mark.gpu
 
 
 def test_many_graphs_bfs_and_pagerank(ctx):
-    specs = batch.workload_a_specs(24, seed=3, min_scale=8, max_scale=13)
-    hosts = [bw.HostGraph.rmat(s["scale"], s["edge_factor"], seed=s["seed"]) for s in specs]
+    specs = batch.workload_a_specs(24, seed=3, min_vertices=200, max_vertices=9000)
+    hosts = [bw.HostGraph.rmat_n(s["n"], s["edge_factor"], seed=s["seed"]) for s in specs]
     packed = batch.pack([bw.DeviceGraph(h, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR) for h in hosts])
     levels, ranks, res = batch.run_graphs(ctx, packed, pr_iterations=20)
     lv_all, pr_all = levels.cpu().numpy(), ranks.cpu().numpy()

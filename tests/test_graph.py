@@ -150,3 +150,27 @@ def test_degree_statistics(kind):
     want = _summary(vals)
     for k in want:
         assert got[k] == pytest.approx(want[k], rel=1e-12, abs=1e-12), k
+
+
+@pytest.mark.parametrize("scale,ef,seed,sym", [(10, 16, 11, False), (12, 8, 5, True), (16, 16, 16, False),
+                                               (13, 32, 2, True)])
+def test_oracle_generator_equals_library_generator(scale, ef, seed, sym):
+    """oracle.generate_rmat (the oracle's own C, used where the product
+    library must not be loaded) gives the library's R-MAT graph bit for bit."""
+    import oracle
+    o = oracle.generate_rmat(scale, ef, seed=seed, symmetrise=sym)
+    h = bw.HostGraph.rmat(scale, ef, seed=seed, symmetrise=sym)
+    for k in ("fwd_vertices", "fwd_edges", "rev_vertices", "rev_edges"):
+        assert np.array_equal(o[k], getattr(h, k)), k
+
+
+@pytest.mark.parametrize("n", [2, 3, 1000, 1500, 4097, 199999])
+def test_rmat_over_any_vertex_count(n):
+    """R-MAT over n vertices: valid CSR of exactly n vertices, the hubs at
+    the low ids like the power-of-two generator's."""
+    g = bw.HostGraph.rmat_n(n, 16, seed=7)
+    assert g.vertex_count == n
+    _check_csr(g)
+    if n >= 1000:
+        deg = np.diff(g.fwd_vertices.astype(np.int64))
+        assert int(np.argmax(deg)) < n // 16

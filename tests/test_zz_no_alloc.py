@@ -44,6 +44,49 @@ def test_noalloc_matches_context_entry_point(ctx):
             assert torch.equal(levels, want.levels)
 
 
+def test_noalloc_at_its_limits(ctx):
+    """A graph at the entry point's size limits: 2^20 vertices and
+    16,776,975 edges.  Vertex 0 points at fifteen hubs and at every leaf;
+    each hub points at every leaf, so level 1 holds fifteen rows of about
+    2^20 edges (the hub-chunk queue's largest load) next to a million leaves."""
+    import torch
+
+    import oracle
+    n = 2 ** 20
+    hubs = np.arange(1, 16, dtype=np.uint32)
+    leaves = np.arange(16, n, dtype=np.uint32)
+    src = np.concatenate([np.zeros(15 + leaves.size, np.uint32), np.repeat(hubs, leaves.size)])
+    dst = np.concatenate([hubs, leaves, np.tile(leaves, hubs.size)])
+    assert src.size == 16 * leaves.size + 15 <= 2 ** 24
+    h = bw.HostGraph.from_edges(n, src, dst)
+    del src, dst
+    g = bw.DeviceGraph(h, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR)
+    want, counts = oracle.bfs(n, h.fwd_vertices, h.fwd_edges, 0)
+    for _ in range(2):
+        levels = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+        rc, count = _noalloc(g, 0, levels)
+        assert rc == 0
+        assert count == len(counts)
+        assert np.array_equal(levels.cpu().numpy(), want)
+
+
+def test_noalloc_second_call_leaves_free_memory_unchanged(ctx):
+    """After the first call on a device (which reserves the fixed array under
+    lazy module loading) a call takes no device memory."""
+    import torch
+    make, root = catalog()["rmat14"]
+    h = make()
+    g = bw.DeviceGraph(h, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR)
+    levels = torch.empty(h.vertex_count, dtype=torch.int32, device="cuda")
+    r = root_of(h, root)
+    assert _noalloc(g, r, levels)[0] == 0
+    torch.cuda.synchronize()
+    before = torch.cuda.mem_get_info()[0]
+    assert _noalloc(g, r, levels)[0] == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == before
+
+
 def test_noalloc_rejects_sizes_beyond_its_maximum():
     # rejected from the sizes alone: no device memory is touched
     view = _abi.GraphView(2 ** 20 + 1, 10, 1, 1, 0, 0, 0, 0, 0, 0)
