@@ -322,6 +322,18 @@ class DeviceGraph:
             _abi._lib.bw_device_graph_free(C.byref(raw))
             self._dev = None
 
+    def degree_statistics(self, ctx: "Context", kind: str = "out", stream=None) -> dict[str, float]:
+        """graph-details statistics (graph-details.cpp:36-61) computed on the
+        device (bw_degree_statistics_device)."""
+        torch = _torch()
+        k = {"abs": 0, "in": 1, "out": 2}[kind]
+        out = (C.c_double * 7)()
+        st = stream or torch.cuda.current_stream(self.device)
+        check(library().bw_degree_statistics_device(ctx.handle, C.byref(self.view), int(self.undirected), k, out,
+                                                    C.c_void_p(st.cuda_stream)), "bw_degree_statistics_device")
+        keys = ["min", "lower", "mean", "median", "upper", "max", "stddev"]
+        return dict(zip(keys, list(out)))
+
     def to_host_arrays(self) -> dict:
         """Copy the forward and reverse CSR back to numpy (uint32)."""
         n, m = self.vertex_count, self.edge_count
@@ -388,12 +400,27 @@ def _stats_list(arr, count):
     return out
 
 
+def _tuned(algorithm: str, variant, g, block, grid, warp, chunk, tuned: bool):
+    """The caller's geometry, or -- when none is given and `tuned` -- the
+    autotuner's configuration for this variant and graph shape class."""
+    if not tuned or block or grid or warp or chunk:
+        return block, grid, warp, chunk
+    from . import autotune
+    name = variant if isinstance(variant, str) else (
+        bfs_variant_names() if algorithm == "bfs" else pagerank_variant_names())[variant]
+    c = autotune.tuned_config(algorithm, name, g)
+    return c.get("block", 0), c.get("grid", 0), c.get("warp", 0), c.get("chunk", 0)
+
+
 def bfs(ctx: Context, g: DeviceGraph, variant: str | int, root: int, *, levels=None,
         loop: str = "host", max_levels: int = 0, stats: bool = False, block: int = 0,
-        grid: int = 0, warp: int = 0, chunk: int = 0, stream=None) -> BfsRun:
-    """BFS from `root` with a fixed variant (BFS::runImplementation)."""
+        grid: int = 0, warp: int = 0, chunk: int = 0, tuned: bool = True, stream=None) -> BfsRun:
+    """BFS from `root` with a fixed variant (BFS::runImplementation).  With
+    no geometry given, the autotuner's configuration for the graph's shape
+    class is used (tuned=False: the library default)."""
     torch = _torch()
     lib = library()
+    block, grid, warp, chunk = _tuned("bfs", variant, g, block, grid, warp, chunk, tuned)
     if levels is None:
         levels = torch.empty(g.vertex_count, dtype=torch.int32, device=f"cuda:{ctx.device}")
     st = stream or torch.cuda.current_stream(levels.device)
@@ -436,10 +463,13 @@ def bfs_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], ro
 
 def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int = 30, *,
              ranks=None, block: int = 0, grid: int = 0, warp: int = 0, chunk: int = 0,
-             relabel: bool | None = None, loop: str = "host", stream=None) -> PageRankRun:
-    """PageRank, damping 0.85, 1/N init, exactly `iterations` iterations."""
+             relabel: bool | None = None, loop: str = "host", tuned: bool = True, stream=None) -> PageRankRun:
+    """PageRank, damping 0.85, 1/N init, exactly `iterations` iterations.
+    With no geometry given, the autotuner's configuration for the graph's
+    shape class is used (tuned=False: the library default)."""
     torch = _torch()
     lib = library()
+    block, grid, warp, chunk = _tuned("pagerank", variant, g, block, grid, warp, chunk, tuned)
     if ranks is None:
         ranks = torch.empty(g.vertex_count, dtype=torch.float32, device=f"cuda:{ctx.device}")
     st = stream or torch.cuda.current_stream(ranks.device)

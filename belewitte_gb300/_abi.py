@@ -97,6 +97,8 @@ SIGNATURES = {
     "bw_graph_file_read": (C.c_int, [C.c_char_p, C.POINTER(HostGraphC)]),
     "bw_graph_file_write": (C.c_int, [C.c_char_p, C.POINTER(HostGraphC)]),
     "bw_degree_statistics": (C.c_int, [C.POINTER(HostGraphC), C.c_int, C.POINTER(C.c_double)]),
+    "bw_degree_statistics_device": (C.c_int, [C.c_void_p, C.POINTER(GraphView), C.c_int, C.c_int,
+                                              C.POINTER(C.c_double), C.c_void_p]),
     "bw_context_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "bw_context_destroy": (C.c_int, [C.c_void_p]),
     "bw_context_sm_count": (C.c_int, [C.c_void_p]),

@@ -60,6 +60,8 @@ def _kind(algorithm: str, name: str) -> str:
 
 
 def candidates(algorithm: str, name: str, sm_count: int):
+    """The library's default launch ({}) first, then the tuning grid."""
+    yield {}
     kind = _kind(algorithm, name)
     blocks = BLOCKS[kind]
     if algorithm == "pagerank" and kind in ("edge", "vertex"):
@@ -75,12 +77,12 @@ def candidates(algorithm: str, name: str, sm_count: int):
 
 
 def _time_bfs(ctx, g, name, root, cfg, repeats):
-    ts = [bfs(ctx, g, name, root, loop="graph", **cfg).device_ms for _ in range(repeats)]
+    ts = [bfs(ctx, g, name, root, loop="graph", tuned=False, **cfg).device_ms for _ in range(repeats)]
     return float(np.median(ts))
 
 
 def _time_pagerank(ctx, g, name, cfg, repeats, iterations):
-    ts = [pagerank(ctx, g, name, iterations, **cfg).device_ms for _ in range(repeats)]
+    ts = [pagerank(ctx, g, name, iterations, tuned=False, **cfg).device_ms for _ in range(repeats)]
     return float(np.median(ts))
 
 
@@ -114,6 +116,24 @@ def tune(ctx, g, algorithm: str, variants=None, *, root: int = 0, repeats: int =
             data.setdefault(algorithm, {}).setdefault(name, {})[cls] = {"config": cfg, "ms": ms}
         cache.parent.mkdir(parents=True, exist_ok=True)
         cache.write_text(json.dumps(data, indent=1, sort_keys=True))
+        export_tsv(cache)
+    return out
+
+
+def export_tsv(cache: Path = CACHE, out: Path | None = None) -> Path:
+    """The per-variant entries of the cache as tab-separated lines
+    `algorithm variant class block grid warp chunk`, the form the C++ plugins
+    read (kernel-runner runs without Python)."""
+    out = out or cache.with_suffix(".tsv")
+    data = json.loads(cache.read_text()) if cache.exists() else {}
+    lines = []
+    for algorithm in ("bfs", "pagerank"):
+        for name, classes in sorted(data.get(algorithm, {}).items()):
+            for cls, entry in sorted(classes.items()):
+                c = entry["config"]
+                lines.append("\t".join([algorithm, name, cls] + [str(int(c.get(k, 0)))
+                                                                  for k in ("block", "grid", "warp", "chunk")]))
+    out.write_text("".join(line + "\n" for line in lines))
     return out
 
 
@@ -128,6 +148,60 @@ def class_distance(a: str, b: str) -> int:
     x = [int(t[1:]) for t in a.split("-")]
     y = [int(t[1:]) for t in b.split("-")]
     return sum(abs(p - q) for p, q in zip(x, y))
+
+
+_loaded: dict = {}
+
+
+def _load(cache: Path) -> dict:
+    """The cache's contents, re-read only when the file changes."""
+    try:
+        stamp = cache.stat().st_mtime_ns
+    except OSError:
+        return {}
+    hit = _loaded.get(cache)
+    if hit is None or hit[0] != stamp:
+        hit = (stamp, json.loads(cache.read_text()))
+        _loaded[cache] = hit
+    return hit[1]
+
+
+def graph_class(g) -> str | None:
+    """shape_class(g), kept on the graph object (None for views without the
+    forward offsets)."""
+    cls = getattr(g, "_shape_class", None)
+    if cls is None:
+        if getattr(g, "fwd_vertices", None) is None or not getattr(g, "vertex_count", 0):
+            return None
+        cls = shape_class(g)
+        try:
+            g._shape_class = cls
+        except AttributeError:
+            pass
+    return cls
+
+
+def tuned_config(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
+    """What bfs() / pagerank() launch a variant with when the caller gives
+    no geometry: the tuned configuration of the graph's shape class (or of
+    the nearest cached class within MAX_CLASS_DISTANCE), else {} -- the
+    library's default."""
+    cls = graph_class(g)
+    if cls is None:
+        return {}
+    entries = _load(cache).get(algorithm, {}).get(name, {})
+    return _nearest(entries, cls)
+
+
+def _nearest(entries: dict, cls: str) -> dict:
+    if not entries:
+        return {}
+    if cls in entries:
+        return dict(entries[cls]["config"])
+    near = min(entries, key=lambda other: class_distance(cls, other))
+    if class_distance(cls, near) > MAX_CLASS_DISTANCE:
+        return {}
+    return dict(entries[near]["config"])
 
 
 def lookup(algorithm: str, name: str, g, cache: Path = CACHE) -> dict:
@@ -199,3 +273,42 @@ def lookup_batch(mode: str, g=None, cache: Path = CACHE) -> int:
     if class_distance(cls, near.split("/", 1)[1]) > MAX_CLASS_DISTANCE:
         return 0
     return int(entries[near]["bu_div"])
+
+
+# ---------------------------------------------------------------------------
+# the shipped cache: every variant on the benchmark configurations' shapes
+# ---------------------------------------------------------------------------
+STANDARD = (
+    ("pagerank", "rmat", dict(scale=22, edge_factor=16, seed=22)),
+    ("pagerank", "er", dict(n=4194304, m=67108864, seed=23)),
+    ("pagerank", "rmat", dict(scale=16, edge_factor=16, seed=16)),
+    ("bfs", "rmat", dict(scale=22, edge_factor=16, seed=22, symmetrise=True)),
+    ("bfs", "rmat", dict(scale=16, edge_factor=16, seed=16)),
+    ("bfs", "ba", dict(n=2097152, m=8, seed=8)),
+)
+
+
+def tune_standard(ctx, cache: Path = CACHE, log=print):
+    """Tune every BFS and PageRank variant on the benchmark configurations'
+    graph shapes (BFS from the highest out-degree vertex; PageRank over 5
+    iterations, enough for the pull variants to take the hub-first order)."""
+    import torch
+
+    from . import DeviceGraph
+    for algorithm, kind, kw in STANDARD:
+        g = DeviceGraph.generate(kind, reps=63, **kw)
+        root = int(torch.argmax(g.fwd_vertices[1:] - g.fwd_vertices[:-1]).item())
+        log(f"{algorithm} on {kind} {kw}: class {shape_class(g)}")
+        tune(ctx, g, algorithm, root=root, cache=cache, log=log)
+        del g
+        torch.cuda.empty_cache()
+
+
+if __name__ == "__main__":
+    import argparse
+
+    from . import Context
+    ap = argparse.ArgumentParser(description="tune every variant on the benchmark graph shapes")
+    ap.add_argument("--cache", default=str(CACHE))
+    a = ap.parse_args()
+    tune_standard(Context(0), cache=Path(a.cache), log=lambda s: print(s, flush=True))

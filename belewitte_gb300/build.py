@@ -27,7 +27,7 @@ INCLUDE = ROOT / "include"
 LIB = PKG / "libbelewitte_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["bw_context.cu", "bfs.cu", "bfs_edge.cu", "bfs_vertex.cu", "pagerank.cu", "bw_gen.cu", "bw_learn.cu", "bw_noalloc.cu", "bw_batch.cu", "bw_probe.cu"]
+CUDA_SOURCES = ["bw_context.cu", "bfs.cu", "bfs_edge.cu", "bfs_vertex.cu", "pagerank.cu", "bw_gen.cu", "bw_learn.cu", "bw_noalloc.cu", "bw_batch.cu", "bw_probe.cu", "bw_stats.cu"]
 CXX_SOURCES = ["bw_graph.cpp"]
 
 

@@ -90,8 +90,8 @@ __global__ void k_bfs_init_side(int32_t *levels, uint64_t n, uint32_t root, uint
             const uint32_t d = outdeg[root];
             const float l = __log2f(1.0f + static_cast<float>(d));
             ctl->slot[2].fedges = d;
-            ctl->slot[2].lsum = l;
-            ctl->slot[2].lsq = l * l;
+            ctl->slot[2].lsum = lsum_fx(l);
+            ctl->slot[2].lsq = lsq_fx(l);
             ctl->slot[2].lmax_bits = __float_as_uint(l);
             ctl->traversed = d;
         }
@@ -231,8 +231,8 @@ void fill_stats(const LevelSlot &s, int variant, bw_bfs_level_stats *out)
     out->frontier_vertices = s.frontier;
     out->variant = static_cast<uint32_t>(variant);
     out->frontier_edges = s.fedges;
-    out->log_degree_sum = s.lsum;
-    out->log_degree_sq_sum = s.lsq;
+    out->log_degree_sum = static_cast<float>(lsum_value(s.lsum));
+    out->log_degree_sq_sum = static_cast<float>(lsq_value(s.lsq));
     uint32_t bits = s.lmax_bits;
     float f;
     std::memcpy(&f, &bits, sizeof f);

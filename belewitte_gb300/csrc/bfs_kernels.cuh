@@ -31,7 +31,7 @@ __device__ __forceinline__ int level_depth(const BfsArgs &a)
 
 __device__ __forceinline__ void reset_slot(LevelSlot *s)
 {
-    s->frontier = 0; s->qlen = 0; s->fedges = 0; s->lsum = 0.f; s->lsq = 0.f;
+    s->frontier = 0; s->qlen = 0; s->fedges = 0; s->lsum = 0; s->lsq = 0;
     s->lmax_bits = 0; s->heavy = 0;
 }
 
@@ -81,14 +81,15 @@ __device__ __forceinline__ void queue_append(uint32_t *q, uint32_t *len, uint32_
 template<bool SIDE>
 struct Side {
     unsigned long long fe = 0;
-    float ls = 0.f, lq = 0.f, lm = 0.f;
+    unsigned long long ls = 0, lq = 0;     // fixed point (lsum_fx, lsq_fx)
+    float lm = 0.f;
     __device__ __forceinline__ void visit(const BfsArgs &a, uint32_t *qnext, LevelSlot *s, uint32_t v)
     {
         if constexpr (SIDE) {
             if (qnext) queue_append(qnext, &s->qlen, v);   // null: statistics only
             const uint32_t d = a.outdeg[v];
             const float l = __log2f(1.0f + static_cast<float>(d));
-            fe += d; ls += l; lq += l * l; lm = fmaxf(lm, l);
+            fe += d; ls += lsum_fx(l); lq += lsq_fx(l); lm = fmaxf(lm, l);
         }
     }
     __device__ __forceinline__ void finish(LevelSlot *s)
@@ -115,7 +116,8 @@ struct Side {
     {
         if constexpr (SIDE) {
             __shared__ unsigned long long b_fe[32];
-            __shared__ float b_ls[32], b_lq[32], b_lm[32];
+            __shared__ unsigned long long b_ls[32], b_lq[32];
+            __shared__ float b_lm[32];
             const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
             for (int o = 16; o > 0; o >>= 1) {
                 fe += __shfl_xor_sync(FULL_MASK, fe, o);
@@ -127,7 +129,7 @@ struct Side {
             __syncthreads();
             if (wid == 0) {
                 const bool in = lane < (blockDim.x >> 5);
-                fe = in ? b_fe[lane] : 0ull; ls = in ? b_ls[lane] : 0.f; lq = in ? b_lq[lane] : 0.f;
+                fe = in ? b_fe[lane] : 0ull; ls = in ? b_ls[lane] : 0ull; lq = in ? b_lq[lane] : 0ull;
                 lm = in ? b_lm[lane] : 0.f;
                 for (int o = 16; o > 0; o >>= 1) {
                     fe += __shfl_xor_sync(FULL_MASK, fe, o);
@@ -730,7 +732,8 @@ struct ClusterCounts {
     uint32_t frontier;            // new vertices of the level found by this block
     uint32_t listed;              // of those, in the block's next list
     unsigned long long fedges;    // their out-edges
-    float ls, lq, lm;             // log-degree statistics (STATS == 1)
+    unsigned long long ls, lq;    // log-degree statistics (STATS == 1), fixed point
+    float lm;
     uint32_t heavy;               // of those, rows above CLUSTER_HEAVY
 };
 
@@ -747,9 +750,10 @@ k_bfs_cluster(BfsArgs a)
     __shared__ uint32_t s_pre[CLUSTER_CTAS + 1];    // exclusive prefix of the blocks' next lists
     __shared__ unsigned long long r_fe[CLUSTER_THREADS / 32];
     __shared__ uint32_t r_hits[CLUSTER_THREADS / 32], r_heavy[CLUSTER_THREADS / 32];
-    __shared__ float r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32], r_lm[CLUSTER_THREADS / 32];
+    __shared__ unsigned long long r_ls[CLUSTER_THREADS / 32], r_lq[CLUSTER_THREADS / 32];
+    __shared__ float r_lm[CLUSTER_THREADS / 32];
     __shared__ uint32_t s_n, s_cur_n;
-    __shared__ float s_hand[3];                    // this block's part of a handed-over frontier's statistics
+    __shared__ unsigned long long s_hand[3];       // this block's part of a handed-over frontier's statistics
     cg::cluster_group cl = cg::this_cluster();
     BfsCtl *ctl = a.ctl;
     const unsigned rank = cl.block_rank(), tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
@@ -807,7 +811,8 @@ k_bfs_cluster(BfsArgs a)
         uint32_t *nv = lst_v[1 + p], *ns = lst_s[1 + p], *ne = lst_e[1 + p];
         uint32_t hits = 0, heavy = 0;
         unsigned long long fe = 0;
-        float ls = 0.f, lq = 0.f, lm = 0.f;
+        unsigned long long ls = 0, lq = 0;
+        float lm = 0.f;
         // a claimed neighbour u with row [us, ue): its counts and its entry k
         auto claim = [&](uint32_t u, uint32_t us, uint32_t ue, uint32_t k) {
             // Next-line prefetch: where vertex ids follow the graph's
@@ -822,7 +827,7 @@ k_bfs_cluster(BfsArgs a)
             heavy += ue - us > CLUSTER_HEAVY ? 1u : 0u;
             if constexpr (STATS == 1) {
                 const float l = __log2f(1.0f + static_cast<float>(ue - us));
-                ls += l; lq += l * l; lm = fmaxf(lm, l);
+                ls += lsum_fx(l); lq += lsq_fx(l); lm = fmaxf(lm, l);
             }
             if (k < CLUSTER_LIST) {
                 nv[k] = u;
@@ -947,23 +952,26 @@ k_bfs_cluster(BfsArgs a)
         __syncthreads();
         const uint32_t f = s_tot.frontier, listed_all = s_tot.listed;
         const unsigned long long fe_all = s_tot.fedges;
-        const float ls_all = s_tot.ls, lq_all = s_tot.lq, lm_all = s_tot.lm;
+        const unsigned long long ls_all = s_tot.ls, lq_all = s_tot.lq;
+        const float lm_all = s_tot.lm;
         if (f == 0 || f > CLUSTER_CAP || fe_all > CLUSTER_EDGE_CAP || listed_all < f || s_tot.heavy ||
             static_cast<uint32_t>(L) + 2 > max_levels) {
             // hand level L to the step kernel: the next queue (overflow first,
             // then the blocks' lists) and the level's slot
             const uint32_t at = (f - listed_all) + s_pre[rank], mine = s_cnt[p].listed;
             for (uint32_t i = tid; i < mine; i += CLUSTER_THREADS) qnext[at + i] = nv[i];
-            float hls = ls_all, hlq = lq_all, hlm = lm_all;
+            unsigned long long hls = ls_all, hlq = lq_all;
+            float hlm = lm_all;
             if constexpr (STATS == 2) {
                 // The handed-over frontier's log-degree statistics: this
                 // block's list entries and its slice of the overflow, which
                 // the other blocks wrote to the global queue before the
                 // counts' cluster barrier (read past L1).
-                float ls = 0.f, lq = 0.f, lm = 0.f;
+                unsigned long long ls = 0, lq = 0;
+                float lm = 0.f;
                 auto add = [&](uint32_t deg) {
                     const float l = __log2f(1.0f + static_cast<float>(deg));
-                    ls += l; lq += l * l; lm = fmaxf(lm, l);
+                    ls += lsum_fx(l); lq += lsq_fx(l); lm = fmaxf(lm, l);
                 };
                 for (uint32_t i = tid; i < mine; i += CLUSTER_THREADS) add(ne[i] - ns[i]);
                 const uint32_t ov = f - listed_all, per = (ov + CLUSTER_CTAS - 1) / CLUSTER_CTAS;
@@ -986,14 +994,16 @@ k_bfs_cluster(BfsArgs a)
                         lq += __shfl_xor_sync(FULL_MASK, lq, o);
                         lm = fmaxf(lm, __shfl_xor_sync(FULL_MASK, lm, o));
                     }
-                    if (lane == 0) { s_hand[0] = ls; s_hand[1] = lq; s_hand[2] = lm; }
+                    if (lane == 0) { s_hand[0] = ls; s_hand[1] = lq; s_hand[2] = __float_as_uint(lm); }
                 }
                 cl.sync();                               // every block's part is out
                 if (leader) {
-                    hls = hlq = hlm = 0.f;
+                    hls = hlq = 0;
+                    hlm = 0.f;
                     for (unsigned q = 0; q < CLUSTER_CTAS; q++) {
-                        const float *h = cl.map_shared_rank(s_hand, q);
-                        hls += h[0]; hlq += h[1]; hlm = fmaxf(hlm, h[2]);
+                        const unsigned long long *h = cl.map_shared_rank(s_hand, q);
+                        hls += h[0]; hlq += h[1];
+                        hlm = fmaxf(hlm, __uint_as_float(static_cast<uint32_t>(h[2])));
                     }
                 }
             }

@@ -1,6 +1,7 @@
 // Internal declarations shared by the CUDA translation units of
 // libbelewitte_gb300.so.  Not part of the C ABI.
 #pragma once
+#include <cmath>
 
 #include <cstdint>
 #include <climits>
@@ -46,11 +47,38 @@ struct LevelSlot {
     uint32_t frontier;            // reference `frontier` counter
     uint32_t qlen;                // next frontier queue length
     unsigned long long fedges;    // sum of out-degrees of new vertices
-    float lsum;                   // sum log2(1+deg)
-    float lsq;                    // sum log2(1+deg)^2
+    unsigned long long lsum;      // sum log2(1+deg), fixed point (lsum_fx)
+    unsigned long long lsq;       // sum log2(1+deg)^2, fixed point (lsq_fx)
     uint32_t lmax_bits;           // max log2(1+deg) as float bits
     uint32_t heavy;               // hub chunks queued (frontier-push)
 };
+
+// The level statistics of log2(1 + out-degree) are summed in fixed point,
+// in units of 2^-24 (sum) and 2^-20 (sum of squares): integer additions are
+// associative, so a level's sums -- and the learned switch's decisions that
+// read them -- are the same whatever order threads, warps and blocks add in.
+// log2(1 + d) <= 32 for 32-bit degrees, so a term is below 2^30 and 2^32
+// terms stay below 2^62.
+constexpr float LSUM_UNIT = 16777216.0f;   // 2^24
+constexpr float LSQ_UNIT = 1048576.0f;     // 2^20
+__host__ __device__ __forceinline__ unsigned long long lsum_fx(float l)
+{
+#if defined(__CUDA_ARCH__)
+    return __float2ull_rn(l * LSUM_UNIT);
+#else
+    return static_cast<unsigned long long>(std::nearbyint(l * LSUM_UNIT));
+#endif
+}
+__host__ __device__ __forceinline__ unsigned long long lsq_fx(float l)
+{
+#if defined(__CUDA_ARCH__)
+    return __float2ull_rn(__fmul_rn(l, l) * LSQ_UNIT);
+#else
+    return static_cast<unsigned long long>(std::nearbyint((l * l) * LSQ_UNIT));
+#endif
+}
+__host__ __device__ __forceinline__ double lsum_value(unsigned long long v) { return static_cast<double>(v) / LSUM_UNIT; }
+__host__ __device__ __forceinline__ double lsq_value(unsigned long long v) { return static_cast<double>(v) / LSQ_UNIT; }
 
 struct BfsCtl {
     LevelSlot slot[3];

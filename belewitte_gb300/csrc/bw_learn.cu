@@ -376,7 +376,8 @@ __global__ void __launch_bounds__(PREDICT_THREADS) k_bfs_predict(PredictArgs a)
         const LevelSlot s = c->slot[(L + 2) % 3];
         float lmax;
         memcpy(&lmax, &s.lmax_bits, 4);
-        bwfeat::compute(static_cast<double>(s.frontier), static_cast<double>(s.fedges), s.lsum, s.lsq, lmax,
+        bwfeat::compute(static_cast<double>(s.frontier), static_cast<double>(s.fedges), lsum_value(s.lsum),
+                        lsq_value(s.lsq), lmax,
                         static_cast<double>(a.n), static_cast<double>(a.m), static_cast<double>(c->visited),
                         static_cast<double>(c->traversed), static_cast<double>(L), x);
     }
@@ -452,8 +453,8 @@ void slot_stats(const LevelSlot &sl, int variant, bw_bfs_level_stats *out)
     out->frontier_vertices = sl.frontier;
     out->variant = static_cast<uint32_t>(variant);
     out->frontier_edges = sl.fedges;
-    out->log_degree_sum = sl.lsum;
-    out->log_degree_sq_sum = sl.lsq;
+    out->log_degree_sum = static_cast<float>(lsum_value(sl.lsum));
+    out->log_degree_sq_sum = static_cast<float>(lsq_value(sl.lsq));
     std::memcpy(&out->log_degree_max, &sl.lmax_bits, 4);
     out->device_ms = 0.0f;
 }
@@ -537,8 +538,8 @@ __global__ void k_bfs_root_stats(const uint32_t *outdeg, uint32_t root, LevelSlo
         out->frontier = 1;
         out->qlen = 1;
         out->fedges = d;
-        out->lsum = l;
-        out->lsq = l * l;
+        out->lsum = lsum_fx(l);
+        out->lsq = lsq_fx(l);
         out->lmax_bits = __float_as_uint(l);
     }
 }
@@ -742,7 +743,8 @@ int bw_bfs_profile(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32
     for (; L < max_levels; L++) {
         float lmax;
         std::memcpy(&lmax, &cur.lmax_bits, 4);
-        bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), cur.lsum, cur.lsq, lmax, static_cast<double>(n),
+        bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_value(cur.lsum), lsq_value(cur.lsq), lmax,
+                        static_cast<double>(n),
                         static_cast<double>(m), static_cast<double>(visited), static_cast<double>(edges_visited), L,
                         features + static_cast<size_t>(L) * F);
         const bool sampled = L < 32 || L % sample_every == 0;
@@ -828,7 +830,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             if (L >= max_levels) { rc = BW_ERR_LEVEL_LIMIT; break; }
             float x[F], probs[BW_MLP_MAX_CLASSES], lmax;
             std::memcpy(&lmax, &cur.lmax_bits, 4);
-            bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), cur.lsum, cur.lsq, lmax,
+            bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_value(cur.lsum), lsq_value(cur.lsq), lmax,
                             static_cast<double>(n), static_cast<double>(m), static_cast<double>(visited),
                             static_cast<double>(edges_visited), L, x);
             mlp_forward_host(hp.data(), K, x, probs);

@@ -75,7 +75,7 @@ struct PrArgs {
     uint32_t warp_size, chunk_size;
     const uint4 *work;         // pull-segmented work items
     uint32_t work_count;
-    uint32_t *long_count;      // arrival counters of split rows
+    uint32_t *long_count;      // arrival counters of long rows (pieces)
     float *vals;               // exact long rows: gathered terms, indexed by edge
     // Hub-first source order (work-list kernels): the gathered array is
     // stored at slot[v] and gat_e holds the reverse-CSR sources translated to
@@ -719,16 +719,16 @@ __global__ void __launch_bounds__(256) k_pr_heavy_finish(PrArgs a)
 // Long rows (more than SEG_LONG edges) are cut into SEG_EDGES-edge pieces
 // that any warp takes; the work list puts every piece, longest rows first,
 // before the short-row items:
-//   EXACT (vertex-pull, vertex-pull-nodiv): pieces store their gathered
+//   staged (vertex-pull, vertex-pull-nodiv): pieces store their gathered
 //   terms in vals[] (edge order); k_pr_long_sums then evaluates every long
 //   row's sequential sum (bit-identical to the reference's loop) and
 //   consolidates it.
-//   split (pull-segmented): pieces add lane partials (shuffle tree) into
-//   acc[] with float atomics; the last piece of the row consolidates it.
+//   inline (pull-segmented): the same sequential sums inside this kernel,
+//   from binade-map records of the pieces (inline_piece); no terms are
+//   staged in global memory and no second kernel runs.
 constexpr uint32_t SEG_EDGES = 512;
 constexpr uint32_t SEG_LONG = 256;
-constexpr uint32_t PIECE_FLAG = 0x80000000u;   // split piece of a long row
-constexpr uint32_t LONG_FLAG = 0x40000000u;    // exact piece of a long row
+constexpr uint32_t LONG_FLAG = 0x40000000u;    // piece of a long row
 constexpr uint32_t CONST_FLAG = 0x20000000u;   // rows without in-edges
 constexpr uint32_t ROW_MASK = 0x1fffffffu;     // work-list variants take N < 2^29
 // Two block shapes: WIDE, one block of 32 warps per SM, and NARROW, blocks
@@ -739,8 +739,12 @@ constexpr uint32_t ROW_MASK = 0x1fffffffu;     // work-list variants take N < 2^
 // from shared memory instead of L2.  Every block holds its own copy, and
 // what shared memory takes is lost to L1, which bounds the misses in flight.
 constexpr int PULL_WIDE = 1024, PULL_NARROW = 256;
-constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (SEG_EDGES + 33) * sizeof(float); }
-constexpr int pull_min_blocks(int block, bool exact) { return block == PULL_WIDE ? 1 : (exact ? 4 : 5); }
+// Per warp: a gather buffer of SEG_EDGES terms, padded to one extra word per
+// 32 (the layout in which a lane reads its own run of terms without bank
+// conflicts), then 33 words of row ends.
+constexpr uint32_t PULL_BUF = SEG_EDGES + SEG_EDGES / 32;
+constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (PULL_BUF + 33) * sizeof(float); }
+constexpr int pull_min_blocks(int block) { return block == PULL_WIDE ? 1 : 4; }
 // default hub-cache entries per block (measured on GB300: WIDE with 16K
 // entries is within 3% of the best shape on both R-MAT-22 and ER(4M, 67M))
 constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
@@ -783,13 +787,22 @@ __global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, co
     }
 }
 
+// Pieces of a long row of n terms.  Staged (vertex-pull, vertex-pull-nodiv):
+// SEG_EDGES terms each.  Inline (pull-segmented): piece 0 is the serial
+// start, the first min(n, SERIAL_TERMS) terms, then SEG_EDGES terms each.
+__host__ __device__ __forceinline__ uint32_t row_pieces(uint32_t n, int inl)
+{
+    if (!inl) return (n + SEG_EDGES - 1) / SEG_EDGES;
+    return n <= SERIAL_TERMS ? 1u : 1u + (n - SERIAL_TERMS + SEG_EDGES - 1) / SEG_EDGES;
+}
+
 // Piece counts of the sorted long rows (0 past the last one).
 __global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
-                              uint64_t cap, uint32_t *__restrict__ pieces)
+                              uint64_t cap, int inl, uint32_t *__restrict__ pieces)
 {
     const uint64_t L = *long_total;
     for (uint64_t i = gtid(); i < cap; i += gthreads())
-        pieces[i] = i < L ? (long_len[i] + SEG_EDGES - 1) / SEG_EDGES : 0u;
+        pieces[i] = i < L ? row_pieces(long_len[i], inl) : 0u;
 }
 
 // Exact long rows above GIANT_ROW terms are summed piece-parallel (binade
@@ -803,7 +816,7 @@ constexpr uint32_t GIANT_ROW = 2048;
 // counters cleared; the number of rows above GIANT_ROW and of their pieces.
 __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ long_row,
                              const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
-                             const uint32_t *__restrict__ ppos, int split, uint4 *__restrict__ work,
+                             const uint32_t *__restrict__ ppos, int inl, uint4 *__restrict__ work,
                              uint32_t *__restrict__ long_count, uint32_t *__restrict__ giant_total,
                              uint32_t *__restrict__ giant_pieces)
 {
@@ -817,12 +830,16 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
         *giant_total = static_cast<uint32_t>(lo);
         *giant_pieces = ppos[lo];
     }
-    const uint32_t flag = split ? PIECE_FLAG : LONG_FLAG;
     for (uint64_t i = gtid(); i < L; i += gthreads()) {
         const uint32_t r = long_row[i];
-        uint32_t out = ppos[i];
-        for (uint32_t p = off[r]; p < off[r + 1]; p += SEG_EDGES)
-            work[out++] = make_uint4(r, (r + 1) | flag, p, min(p + SEG_EDGES, off[r + 1]));
+        uint32_t out = ppos[i], p = off[r];
+        if (inl) {                                   // the serial start
+            const uint32_t e = min(p + SERIAL_TERMS, off[r + 1]);
+            work[out++] = make_uint4(r, (r + 1) | LONG_FLAG, p, e);
+            p = e;
+        }
+        for (; p < off[r + 1]; p += SEG_EDGES)
+            work[out++] = make_uint4(r, (r + 1) | LONG_FLAG, p, min(p + SEG_EDGES, off[r + 1]));
         long_count[r] = 0;
     }
 }
@@ -995,141 +1012,10 @@ __device__ __noinline__ float warp_plain_sum(const float *vals, uint32_t n, unsi
     return __shfl_sync(FULL_MASK, s, 0);
 }
 
-template<bool NODIV, bool EXACT_LONG, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK, EXACT_LONG)) k_pr_pull_items(PrArgs a)
-{
-    constexpr int PULL_WARPS = BLOCK / 32;
-    resolve_args(a);
-    extern __shared__ __align__(16) float smem_f[];
-    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
-    const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
-    const uint32_t *ge = a.gat_e;
-    const float base_nd = nodiv_base(a.n);
-    float *buf = smem_f + wib * SEG_EDGES;
-    uint32_t *s_end = reinterpret_cast<uint32_t *>(smem_f + PULL_WARPS * SEG_EDGES) + wib * 33;
-    float *hub = smem_f + PULL_WARPS * (SEG_EDGES + 33);
-    const uint32_t hubs = a.hub_count;       // multiple of 4
-    for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
-        reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
-    __syncthreads();
-    float dsum = 0.0f;
-    // the next item's descriptor is loaded one item ahead
-    uint4 w_next = warp < a.work_count ? a.work[warp] : make_uint4(0, 0, 0, 0);
-    for (uint64_t it = warp; it < a.work_count; it += warps) {
-        const uint4 w = w_next;
-        if (it + warps < a.work_count) w_next = a.work[it + warps];
-        const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
-        if (!EXACT_LONG && (w.y & PIECE_FLAG)) {
-            float part = 0.0f;
-            for (uint32_t base = e0; base < e1; base += 32 * GATHER_UNROLL) {
-                uint32_t idx[GATHER_UNROLL];
-#pragma unroll
-                for (int u = 0; u < GATHER_UNROLL; u++) {
-                    const uint32_t i = base + u * 32 + lane;
-                    idx[u] = i < e1 ? __ldcs(ge + i) : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < GATHER_UNROLL; u++) {
-                    const uint32_t i = base + u * 32 + lane;
-                    part += i < e1 ? gather1(src, hub, hubs, idx[u]) : 0.0f;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
-            if (lane == 0) {
-                atomicAdd(&a.acc[r0], part);
-                __threadfence();
-                const uint32_t pieces = (a.rev_v[r0 + 1] - a.rev_v[r0] + SEG_EDGES - 1) / SEG_EDGES;
-                if (atomicAdd(&a.long_count[r0], 1u) + 1 == pieces) {
-                    __threadfence();
-                    const float total = atomicExch(&a.acc[r0], 0.0f);
-                    a.long_count[r0] = 0;
-                    dsum += finish_vertex<NODIV>(a, r0, total, base_nd);
-                }
-            }
-            continue;
-        }
-        if (EXACT_LONG && (w.y & LONG_FLAG)) {
-            // exact piece: store the gathered terms in edge order (the
-            // long-row sums run in k_pr_long_sums after this kernel) and
-            // their float sum in any order, from which the pieces of giant
-            // rows guess the running sum of the row
-            const uint32_t len = e1 - e0;
-            float part = 0.0f;
-            for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
-                uint32_t idx[GATHER_UNROLL];
-#pragma unroll
-                for (int u = 0; u < GATHER_UNROLL; u++) {
-                    const uint32_t k = base + u * 32 + lane;
-                    idx[u] = k < len ? __ldcs(ge + e0 + k) : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < GATHER_UNROLL; u++) {
-                    const uint32_t k = base + u * 32 + lane;
-                    if (k < len) {
-                        const float v = gather1(src, hub, hubs, idx[u]);
-                        __stcg(a.vals + e0 + k, v);
-                        part += v;
-                    }
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
-            if (lane == 0) a.piece_sum[it] = part;   // pieces lead the list: item = piece
-            continue;
-        }
-        // up to 32 rows rows[r0 + l]: lane l owns one; its row end and
-        // consolidation inputs are loaded alongside the gathers
-        const uint32_t rows = r1 - r0, len = e1 - e0;
-        uint32_t row = 0;
-        FinishIn fin{0.0f, 0u, 0u};
-        if (lane < rows) {
-            row = a.rows[r0 + lane];
-            fin = finish_load<NODIV>(a, row);
-        }
-        if (w.y & CONST_FLAG) {                            // no in-edges: the sum is +0
-            if (lane < rows) dsum += finish_store<NODIV>(a, row, 0.0f, base_nd, fin);
-            continue;
-        }
-        if (lane < rows) s_end[lane] = a.rev_v[row + 1] - e0;
-        gather_into(ge, src, hub, hubs, e0, len, buf, lane);
-        __syncwarp();
-        if (lane < rows) {
-            const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
-            float sum = 0.0f;
-            for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
-            dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
-        }
-        __syncwarp();
-    }
-    add_diff(a.diff, dsum);
-}
-
-// Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
-// after the iteration's work-list kernel has stored every long row's terms
-// in vals[] (edge order) and every piece's float sum in piece_sum[].  Jobs
-// are taken in order from a counter (no static share, so a warp that drew a
-// long job takes fewer):
-//  * first batches of 32 long rows of at most GIANT_ROW terms and similar
-//    length, one row per lane (lane_sequential_sum): the longest chains of
-//    dependent additions start first.
-//  * then the pieces of the rows above GIANT_ROW terms, longest rows
-//    first.  Piece 0 adds the row's first SERIAL_TERMS terms in order (one
-//    lane, from shared memory).  Every later piece guesses the running sum at its start (the
-//    float sums of the pieces before it, added in double) and records, in
-//    the guessed binade, the map of its terms -- or, when the guess crosses
-//    into the next binade inside the piece, the map of the terms before the
-//    crossing term, that term, and the map of the terms after it in the new
-//    binade.  The row's last piece to finish combines the records in order,
-//    scanning runs of map records with the warp: a record that holds for
-//    the true running sum (same binade, crossing where recorded) is applied,
-//    any other piece is evaluated exactly from the true running sum
-//    (warp_sequential_continue).  The guesses only decide how much work the
-//    combination does, never its result.
-// Every sum is the reference's sequential loop, bit-identical.  The last
-// warp to finish resets the job counters for the next iteration; each
-// giant row's combining piece resets the row's arrival counter.
-constexpr int LONG_SUM_THREADS = 256;
-constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
+// --------------- binade-map records of long-row pieces -------------------
+// Shared by k_pr_long_sums (vertex-pull, vertex-pull-nodiv: terms staged in
+// vals[]) and the fused pull-segmented kernel (terms gathered into the
+// warp's shared-memory buffer).
 constexpr uint32_t PIECE_L = SEG_EDGES / 32;        // terms per lane: one window per piece
 constexpr uint32_t SERIAL_PIECES = SERIAL_TERMS / SEG_EDGES;
 static_assert(SERIAL_TERMS % SEG_EDGES == 0, "the serial start covers whole pieces");
@@ -1210,46 +1096,16 @@ __device__ __forceinline__ bwseq::Map lane_maps(const uint32_t (&x)[PIECE_L], ui
     return saturated(t[0]);
 }
 
-// The record of piece q >= SERIAL_PIECES of a giant row (valid in lane 0).
-__device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0, uint32_t q,
-                                             float *stage, unsigned lane, uint4 &r0, uint4 &r1)
+// The record of a piece's terms under the guessed running sum `guess` at
+// its start (valid in lane 0): lane l holds the piece's terms l * PIECE_L
+// .. l * PIECE_L + PIECE_L - 1 (past the piece's end: +0, the identity).
+// REC_NONE when the guess or a term is outside the maps' domain.
+__device__ __forceinline__ void record_of_terms(const uint32_t (&x)[PIECE_L], uint32_t guess, unsigned lane,
+                                                uint4 &r0, uint4 &r1)
 {
     using namespace bwseq;
     r0 = make_uint4(REC_NONE, 0u, 0u, 0u);
     r1 = make_uint4(0u, 0u, 0u, 0u);
-    const uint32_t b = q * SEG_EDGES, len = min(SEG_EDGES, n - b);
-    float v[PIECE_L];                                // the terms, coalesced (issued first)
-#pragma unroll
-    for (uint32_t u = 0; u < PIECE_L; u++) {
-        const uint32_t k = u * 32 + lane;
-        v[u] = k < len ? __ldcg(rv + b + k) : 0.0f;
-    }
-    constexpr uint32_t PRE_U = 4;                    // the guess: earlier pieces' sums in double
-    double pre = 0.0;
-    for (uint32_t i0 = 0; i0 < q; i0 += 32 * PRE_U) {
-        float f[PRE_U];
-#pragma unroll
-        for (uint32_t k = 0; k < PRE_U; k++) {
-            const uint32_t i = i0 + k * 32 + lane;
-            f[k] = i < q ? __ldcg(a.piece_sum + p0 + i) : 0.0f;
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < PRE_U; k++) pre += static_cast<double>(f[k]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
-    // restage so that lane l holds terms l*PIECE_L .. (element k at k + k / 32)
-#pragma unroll
-    for (uint32_t u = 0; u < PIECE_L; u++) stage[u * 33 + lane] = v[u];
-    __syncwarp();
-    uint32_t x[PIECE_L];
-#pragma unroll
-    for (uint32_t u = 0; u < PIECE_L; u++) {
-        const uint32_t k = lane * PIECE_L + u;
-        x[u] = __float_as_uint(stage[k + (k >> 5)]);   // past the end: +0, the identity
-    }
-    __syncwarp();
-    const uint32_t guess = __float_as_uint(__double2float_rn(pre));
     if (!in_domain(guess)) return;
     const uint32_t K = exponent_of(guess), first = lane * PIECE_L;
     bool good = true;
@@ -1306,6 +1162,49 @@ __device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, u
     r1 = make_uint4(xb, m2.e, m2.o, 0u);
 }
 
+// The record of piece q >= SERIAL_PIECES of a giant row (valid in lane 0).
+__device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0, uint32_t q,
+                                             float *stage, unsigned lane, uint4 &r0, uint4 &r1)
+{
+    using namespace bwseq;
+    r0 = make_uint4(REC_NONE, 0u, 0u, 0u);
+    r1 = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t b = q * SEG_EDGES, len = min(SEG_EDGES, n - b);
+    float v[PIECE_L];                                // the terms, coalesced (issued first)
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) {
+        const uint32_t k = u * 32 + lane;
+        v[u] = k < len ? __ldcg(rv + b + k) : 0.0f;
+    }
+    constexpr uint32_t PRE_U = 4;                    // the guess: earlier pieces' sums in double
+    double pre = 0.0;
+    for (uint32_t i0 = 0; i0 < q; i0 += 32 * PRE_U) {
+        float f[PRE_U];
+#pragma unroll
+        for (uint32_t k = 0; k < PRE_U; k++) {
+            const uint32_t i = i0 + k * 32 + lane;
+            f[k] = i < q ? __ldcg(a.piece_sum + p0 + i) : 0.0f;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < PRE_U; k++) pre += static_cast<double>(f[k]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
+    // restage so that lane l holds terms l*PIECE_L .. (element k at k + k / 32)
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) stage[u * 33 + lane] = v[u];
+    __syncwarp();
+    uint32_t x[PIECE_L];
+#pragma unroll
+    for (uint32_t u = 0; u < PIECE_L; u++) {
+        const uint32_t k = lane * PIECE_L + u;
+        x[u] = __float_as_uint(stage[k + (k >> 5)]);   // past the end: +0, the identity
+    }
+    __syncwarp();
+    const uint32_t guess = __float_as_uint(__double2float_rn(pre));
+    record_of_terms(x, guess, lane, r0, r1);
+}
+
 // The exact evaluation of piece q from the running sum `sb` (rare: kept
 // out of line, so that the kernel's frequent paths stay small in the
 // instruction cache).  Returns {ok, new sb}.
@@ -1320,8 +1219,9 @@ __device__ __noinline__ uint2 piece_exact(const float *rv, uint32_t n, uint32_t 
 // Piece q from the running sum `sb`: its record when it holds for that sum,
 // else the exact evaluation of its terms.  False when a term or the sum
 // leaves the maps' domain.
-__device__ __forceinline__ bool piece_advance(const float *rv, uint32_t n, uint32_t q, const uint4 &r0,
-                                              const uint4 &r1, uint32_t &sb, float *stage, unsigned lane)
+// exact(q, sb) evaluates piece q from sb and returns {ok, new sb}.
+template<class Exact>
+__device__ __forceinline__ bool piece_advance(uint32_t q, const uint4 &r0, const uint4 &r1, uint32_t &sb, Exact exact)
 {
     using namespace bwseq;
     const uint32_t kind = r0.x & 0xffu, K = r0.y & 0xffu;
@@ -1344,23 +1244,26 @@ __device__ __forceinline__ bool piece_advance(const float *rv, uint32_t n, uint3
             }
         }
     }
-    const uint2 r = piece_exact(rv, n, q, sb, stage, lane);
+    const uint2 r = exact(q, sb);
     sb = r.y;
     return r.x != 0;
 }
 
-// The row's sum from the records of its pieces p0 .. p0 + pieces - 1 (the
-// warp of the last piece to finish).  Groups of 32 records: the run of map
-// records in the current sum's binade is applied with one scan, up to the
-// first piece it cannot take, which piece_advance takes.
-__device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0,
-                                                uint32_t pieces, float *stage, unsigned lane)
+// The row's sum from the records rec[0 .. pieces) of its pieces (the warp
+// of the last piece to finish): rec[0] holds the running sum after the
+// serial start (REC_STATE), map records begin at piece `first`.  Groups of
+// 32 records: the run of map records in the current sum's binade is
+// applied with one scan, up to the first piece it cannot take, which
+// piece_advance takes (exact(q, sb) evaluates piece q from sb; plain() is
+// the whole row's plain loop, for terms outside the maps' domain).
+template<class Exact, class Plain>
+__device__ __forceinline__ float combine_records(const uint4 *rec, uint32_t first, uint32_t pieces, unsigned lane,
+                                                 Exact exact, Plain plain)
 {
     using namespace bwseq;
-    const uint4 *rec = a.piece_map + 2 * static_cast<uint64_t>(p0);
     uint32_t sb = __ldcg(rec).y;                     // REC_STATE of piece 0
     bool ok = true;
-    for (uint32_t g = SERIAL_PIECES; g < pieces && ok; g += 32) {
+    for (uint32_t g = first; g < pieces && ok; g += 32) {
         const uint32_t cnt = min(32u, pieces - g);
         const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
         const uint4 r0 = lane < cnt ? __ldcg(rec + 2 * (g + lane)) : zero;
@@ -1385,13 +1288,298 @@ __device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv
                            __shfl_sync(FULL_MASK, r0.z, s), __shfl_sync(FULL_MASK, r0.w, s)};
             const uint4 q1{__shfl_sync(FULL_MASK, r1.x, s), __shfl_sync(FULL_MASK, r1.y, s),
                            __shfl_sync(FULL_MASK, r1.z, s), __shfl_sync(FULL_MASK, r1.w, s)};
-            ok = piece_advance(rv, n, g + s, q0, q1, sb, stage, lane);
+            ok = piece_advance(g + s, q0, q1, sb, exact);
             pos = s + 1;
         }
     }
-    return ok ? __uint_as_float(sb) : warp_plain_sum(rv, n, lane);
+    return ok ? __uint_as_float(sb) : plain();
 }
 
+// k_pr_long_sums: the records of a giant row whose terms are in vals[].
+__device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv, uint32_t n, uint32_t p0,
+                                                uint32_t pieces, float *stage, unsigned lane)
+{
+    return combine_records(a.piece_map + 2 * static_cast<uint64_t>(p0), SERIAL_PIECES, pieces, lane,
+                           [&](uint32_t q, uint32_t sb) { return piece_exact(rv, n, q, sb, stage, lane); },
+                           [&]() { return warp_plain_sum(rv, n, lane); });
+}
+
+
+// ------------------ pull-segmented: long rows summed inline -----------------
+// Every long row's sequential sum inside the work-list kernel, bit-identical
+// to the reference's loop, with no terms staged in global memory:
+//  * Piece 0 covers the row's first min(n, SERIAL_TERMS) terms.  The warp
+//    gathers them SEG_EDGES at a time into its buffer and lane 0 adds them in
+//    row order; a row of at most SERIAL_TERMS terms ends there.
+//  * Every later piece (SEG_EDGES terms) gathers its terms into the padded
+//    layout, posts their float sum (any order) in psum[], waits for the sums
+//    of the row's earlier pieces -- neighbours in the list, processed in the
+//    same round by other warps -- and records the map of its terms under the
+//    guess those sums give, added in double (record_of_terms).  Piece 0 posts
+//    the exact running sum after the serial start.
+//  * The row's last piece to arrive combines the records in order
+//    (combine_records); a piece whose record does not hold for the true
+//    running sum is evaluated exactly by gathering its terms again.
+// A wait is bounded: one that runs out (warps not all resident, e.g. a
+// caller's grid larger than one wave) leaves its piece without a record, and
+// the combination evaluates that piece exactly, so the limit costs time,
+// never a different result.
+constexpr uint32_t PSUM_EMPTY = 0xffffffffu;       // a NaN: no sum posted yet
+constexpr uint32_t PSUM_SPIN_LIMIT = 1u << 16;
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
+// Gather src[ge[e0 + k]], k < len <= SEG_EDGES, into buf at k + k / 32 (the
+// padded layout record_of_terms reads without bank conflicts); the slots
+// past len up to SEG_EDGES get +0.  Returns this lane's partial sum.
+__device__ __forceinline__ float gather_padded(const uint32_t *__restrict__ ge, const float *__restrict__ src,
+                                               const float *hub, uint32_t hubs, uint32_t e0, uint32_t len,
+                                               float *buf, unsigned lane)
+{
+    static_assert(GATHER_UNROLL * 32 == SEG_EDGES, "one gather round per piece");
+    uint32_t idx[GATHER_UNROLL];
+#pragma unroll
+    for (int u = 0; u < GATHER_UNROLL; u++) {
+        const uint32_t k = u * 32 + lane;
+        idx[u] = k < len ? __ldcs(ge + e0 + k) : 0u;
+    }
+    float part = 0.0f;
+#pragma unroll
+    for (int u = 0; u < GATHER_UNROLL; u++) {
+        const uint32_t k = u * 32 + lane;
+        const float v = k < len ? gather1(src, hub, hubs, idx[u]) : 0.0f;
+        buf[k + (k >> 5)] = v;
+        part += v;
+    }
+    return part;
+}
+
+template<bool NODIV>
+__device__ __noinline__ void inline_piece(const PrArgs &a, uint32_t item, uint32_t row, uint32_t e0, uint32_t e1,
+                                             const float *src, const float *hub, uint32_t hubs, float *buf,
+                                             unsigned lane, float base_nd, float &dsum)
+{
+    using namespace bwseq;
+    const uint32_t *ge = a.gat_e;
+    const uint32_t rb = a.rev_v[row], n = a.rev_v[row + 1] - rb;
+    const uint32_t pieces = row_pieces(n, 1);
+    const uint32_t q = e0 == rb ? 0u : 1u + (e0 - rb - SERIAL_TERMS) / SEG_EDGES;
+    const uint32_t p0 = item - q;
+    uint32_t *psum = reinterpret_cast<uint32_t *>(a.piece_sum);
+    uint4 r0 = make_uint4(REC_NONE, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
+    if (q == 0) {
+        // the serial start, in row order by lane 0 (four terms per load)
+        float acc = 0.0f;
+        for (uint32_t b = e0; b < e1; b += SEG_EDGES) {
+            const uint32_t len = min(SEG_EDGES, e1 - b);
+            gather_into(ge, src, hub, hubs, b, len, buf, lane);
+            __syncwarp();
+            if (lane == 0) {
+                const float4 *b4 = reinterpret_cast<const float4 *>(buf);
+                uint32_t k = 0;
+#pragma unroll 4
+                for (; k + 4 <= len; k += 4) {
+                    const float4 v = b4[k / 4];
+                    acc = __fadd_rn(acc, v.x); acc = __fadd_rn(acc, v.y);
+                    acc = __fadd_rn(acc, v.z); acc = __fadd_rn(acc, v.w);
+                }
+                for (; k < len; k++) acc = __fadd_rn(acc, buf[k]);
+            }
+            __syncwarp();
+        }
+        if (pieces == 1) {
+            if (lane == 0) dsum += finish_vertex<NODIV>(a, row, acc, base_nd);
+            return;
+        }
+        const uint32_t sb = __shfl_sync(FULL_MASK, __float_as_uint(acc), 0);
+        if (lane == 0) st_release_u32(psum + item, sb);
+        r0 = make_uint4(REC_STATE, sb, 0u, 0u);
+    } else {
+        float part = gather_padded(ge, src, hub, hubs, e0, e1 - e0, buf, lane);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
+        if (lane == 0) st_release_u32(psum + item, __float_as_uint(part));
+        // the guess: the earlier pieces' sums, posted by the warps holding them
+        double pre = 0.0;
+        bool ready = true;
+        for (uint32_t i0 = 0; i0 < q && ready; i0 += 32) {
+            uint32_t bits = 0u;
+            if (i0 + lane < q) {
+                uint32_t spins = 0;
+                while ((bits = ld_acquire_u32(psum + p0 + i0 + lane)) == PSUM_EMPTY && ++spins < PSUM_SPIN_LIMIT)
+                    __nanosleep(32);
+            }
+            ready = __all_sync(FULL_MASK, bits != PSUM_EMPTY);
+            pre += static_cast<double>(__uint_as_float(bits));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
+        __syncwarp();                                 // the gathered terms are in buf
+        if (ready) {
+            uint32_t x[PIECE_L];
+#pragma unroll
+            for (uint32_t u = 0; u < PIECE_L; u++) {
+                const uint32_t k = lane * PIECE_L + u;
+                x[u] = __float_as_uint(buf[k + (k >> 5)]);
+            }
+            record_of_terms(x, __float_as_uint(__double2float_rn(pre)), lane, r0, r1);
+        }
+        __syncwarp();
+    }
+    uint32_t last = 0;
+    if (lane == 0) {
+        a.piece_map[2 * static_cast<uint64_t>(item)] = r0;
+        a.piece_map[2 * static_cast<uint64_t>(item) + 1] = r1;
+        last = atomic_add_acq_rel(&a.long_count[row], 1u) + 1 == pieces ? 1u : 0u;
+    }
+    if (!__shfl_sync(FULL_MASK, last, 0)) return;
+    __syncwarp();                                     // every lane's reads after lane 0's acquire
+    const float total = combine_records(
+        a.piece_map + 2 * static_cast<uint64_t>(p0), 1u, pieces, lane,
+        [&](uint32_t qq, uint32_t sb) {
+            const uint32_t b = SERIAL_TERMS + (qq - 1) * SEG_EDGES;
+            const bool ok = warp_sequential_continue_load<PIECE_L>(
+                [&](uint32_t i) { return gather1(src, hub, hubs, __ldcg(ge + rb + i)); },
+                b, min(n, b + SEG_EDGES), sb, buf, lane);
+            return make_uint2(ok ? 1u : 0u, sb);
+        },
+        [&]() {                                       // terms outside the maps' domain
+            float t = 0.0f;
+            if (lane == 0)
+                for (uint32_t i = 0; i < n; i++) t = __fadd_rn(t, gather1(src, hub, hubs, __ldcg(ge + rb + i)));
+            return __shfl_sync(FULL_MASK, t, 0);
+        });
+    if (lane == 0) {
+        dsum += finish_vertex<NODIV>(a, row, total, base_nd);
+        a.long_count[row] = 0;
+    }
+    for (uint32_t i = lane; i < pieces; i += 32) psum[p0 + i] = PSUM_EMPTY;   // for the next iteration
+}
+
+// Long rows of the work-list kernel: staged in vals[] for k_pr_long_sums
+// (vertex-pull, vertex-pull-nodiv) or summed inline (pull-segmented).
+constexpr int LONG_STAGED = 1, LONG_INLINE = 2;
+
+template<bool NODIV, int MODE, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items(PrArgs a)
+{
+    constexpr int PULL_WARPS = BLOCK / 32;
+    resolve_args(a);
+    extern __shared__ __align__(16) float smem_f[];
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
+    const uint32_t *ge = a.gat_e;
+    const float base_nd = nodiv_base(a.n);
+    float *buf = smem_f + wib * PULL_BUF;
+    uint32_t *s_end = reinterpret_cast<uint32_t *>(smem_f + PULL_WARPS * PULL_BUF) + wib * 33;
+    float *hub = smem_f + PULL_WARPS * (PULL_BUF + 33);
+    const uint32_t hubs = a.hub_count;       // multiple of 4
+    for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
+        reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
+    __syncthreads();
+    float dsum = 0.0f;
+    // the next item's descriptor is loaded one item ahead
+    uint4 w_next = warp < a.work_count ? a.work[warp] : make_uint4(0, 0, 0, 0);
+    for (uint64_t it = warp; it < a.work_count; it += warps) {
+        const uint4 w = w_next;
+        if (it + warps < a.work_count) w_next = a.work[it + warps];
+        const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
+        if (MODE == LONG_INLINE && (w.y & LONG_FLAG)) {
+            inline_piece<NODIV>(a, static_cast<uint32_t>(it), r0, e0, e1, src, hub, hubs, buf, lane, base_nd, dsum);
+            continue;
+        }
+        if (MODE == LONG_STAGED && (w.y & LONG_FLAG)) {
+            // exact piece: store the gathered terms in edge order (the
+            // long-row sums run in k_pr_long_sums after this kernel) and
+            // their float sum in any order, from which the pieces of giant
+            // rows guess the running sum of the row
+            const uint32_t len = e1 - e0;
+            float part = 0.0f;
+            for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
+                uint32_t idx[GATHER_UNROLL];
+#pragma unroll
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t k = base + u * 32 + lane;
+                    idx[u] = k < len ? __ldcs(ge + e0 + k) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < GATHER_UNROLL; u++) {
+                    const uint32_t k = base + u * 32 + lane;
+                    if (k < len) {
+                        const float v = gather1(src, hub, hubs, idx[u]);
+                        __stcg(a.vals + e0 + k, v);
+                        part += v;
+                    }
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
+            if (lane == 0) a.piece_sum[it] = part;   // pieces lead the list: item = piece
+            continue;
+        }
+        // up to 32 rows rows[r0 + l]: lane l owns one; its row end and
+        // consolidation inputs are loaded alongside the gathers
+        const uint32_t rows = r1 - r0, len = e1 - e0;
+        uint32_t row = 0;
+        FinishIn fin{0.0f, 0u, 0u};
+        if (lane < rows) {
+            row = a.rows[r0 + lane];
+            fin = finish_load<NODIV>(a, row);
+        }
+        if (w.y & CONST_FLAG) {                            // no in-edges: the sum is +0
+            if (lane < rows) dsum += finish_store<NODIV>(a, row, 0.0f, base_nd, fin);
+            continue;
+        }
+        if (lane < rows) s_end[lane] = a.rev_v[row + 1] - e0;
+        gather_into(ge, src, hub, hubs, e0, len, buf, lane);
+        __syncwarp();
+        if (lane < rows) {
+            const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
+            float sum = 0.0f;
+            for (uint32_t i = b; i < e; i++) sum = __fadd_rn(sum, buf[i]);
+            dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
+        }
+        __syncwarp();
+    }
+    add_diff(a.diff, dsum);
+}
+
+// Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
+// after the iteration's work-list kernel has stored every long row's terms
+// in vals[] (edge order) and every piece's float sum in piece_sum[].  Jobs
+// are taken in order from a counter (no static share, so a warp that drew a
+// long job takes fewer):
+//  * first batches of 32 long rows of at most GIANT_ROW terms and similar
+//    length, one row per lane (lane_sequential_sum): the longest chains of
+//    dependent additions start first.
+//  * then the pieces of the rows above GIANT_ROW terms, longest rows
+//    first.  Piece 0 adds the row's first SERIAL_TERMS terms in order (one
+//    lane, from shared memory).  Every later piece guesses the running sum at its start (the
+//    float sums of the pieces before it, added in double) and records, in
+//    the guessed binade, the map of its terms -- or, when the guess crosses
+//    into the next binade inside the piece, the map of the terms before the
+//    crossing term, that term, and the map of the terms after it in the new
+//    binade.  The row's last piece to finish combines the records in order,
+//    scanning runs of map records with the warp: a record that holds for
+//    the true running sum (same binade, crossing where recorded) is applied,
+//    any other piece is evaluated exactly from the true running sum
+//    (warp_sequential_continue).  The guesses only decide how much work the
+//    combination does, never its result.
+// Every sum is the reference's sequential loop, bit-identical.  The last
+// warp to finish resets the job counters for the next iteration; each
+// giant row's combining piece resets the row's arrival counter.
+constexpr int LONG_SUM_THREADS = 256;
+constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
 template<bool NODIV>
 __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr_long_sums(PrArgs a, uint32_t *ctr)
 {
@@ -1486,7 +1674,7 @@ int check_reps(const bw_graph_view *g, int reps)
 // Per-run state of one PageRank execution.
 struct PrRun {
     uint4 *work = nullptr;
-    uint32_t *long_count = nullptr;    // split: arrival counters per long row
+    uint32_t *long_count = nullptr;    // arrival counters per long row
     uint32_t *scratch = nullptr;       // every other per-run array (one allocation)
     float *vals = nullptr;             // exact long rows: gathered terms (edge-indexed)
     uint32_t *rows = nullptr;          // rows with in-edges, then rows without
@@ -1508,9 +1696,8 @@ Geometry geometry(const bw_context *ctx, int variant, const bw_launch_config *cf
     Geometry g{256, static_cast<unsigned>(ctx->sm_count) * 8, 0};
     if (variant == PR_PULL_SEGMENTED || variant == PR_VERTEX_PULL || variant == PR_VERTEX_PULL_NODIV) {
         // block_size picks the shape (default WIDE); one resident wave
-        const bool exact = variant != PR_PULL_SEGMENTED;
         g.block = (cfg && cfg->block_size == PULL_NARROW) ? PULL_NARROW : PULL_WIDE;
-        g.grid = static_cast<unsigned>(ctx->sm_count) * pull_min_blocks(static_cast<int>(g.block), exact);
+        g.grid = static_cast<unsigned>(ctx->sm_count) * pull_min_blocks(static_cast<int>(g.block));
         if (cfg && cfg->grid_size) g.grid = cfg->grid_size;
         g.smem = pull_fixed_smem(static_cast<int>(g.block));  // + the hub cache (run_pagerank)
         return g;
@@ -1586,7 +1773,7 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
     return BW_OK;
 }
 
-int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &run, cudaStream_t s)
+int build_segments(bw_context *ctx, const bw_graph_view *g, int inl, PrRun &run, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count, m = g->edge_count;
     if (n > ROW_MASK) return BW_ERR_TOO_LARGE;
@@ -1647,11 +1834,11 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     lids = cub::DoubleBuffer<uint32_t>(S + o_lid0, S + o_lid1);
     BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
     run.long_rows = lids.Current();
-    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, pcnt);
+    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, inl, pcnt);
     BW_CUDA(cudaMemsetAsync(pcnt + lcap, 0, sizeof(uint32_t), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
-                                      split, run.work, run.long_count, run.giant_total, run.giant_pieces);
+                                      inl, run.work, run.long_count, run.giant_total, run.giant_pieces);
     BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
     k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, wcnt);
@@ -1662,11 +1849,13 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int split, PrRun &ru
     BW_CUDA(cudaGetLastError());
     run.count_nonconst = tot;
     run.count_all = tot + 1;
-    if (!split && m) {
-        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
+    if (m) {
+        if (!inl) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
         const uint64_t pcap = m / SEG_EDGES + lcap + 1;     // pieces at most
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_map), 2 * pcap * sizeof(uint4), s));
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_sum), pcap * sizeof(float), s));
+        // inline: every posted piece sum starts empty (PSUM_EMPTY)
+        if (inl) BW_CUDA(cudaMemsetAsync(run.piece_sum, 0xff, pcap * sizeof(float), s));
     }
     return BW_OK;
 }
@@ -1701,14 +1890,14 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches++;
         break;
       case PR_VERTEX_PULL:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, LONG_STAGED, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, LONG_STAGED, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_NODIV:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<true, true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<true, true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        if (geo.block == PULL_WIDE) k_pr_pull_items<true, LONG_STAGED, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<true, LONG_STAGED, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         k_pr_long_sums<true><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
@@ -1725,8 +1914,8 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches += 2;
         break;
       case PR_PULL_SEGMENTED:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, LONG_INLINE, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, LONG_INLINE, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         break;
       default: return BW_ERR_UNKNOWN_VARIANT;
     }
@@ -1841,7 +2030,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         return BW_ERR_INVALID_ARGUMENT;
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
-    bool need_split = false, need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
+    bool need_inline = false, need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
          all_items = true;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
@@ -1850,7 +2039,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         if (is_nodiv(v) != nodiv) return BW_ERR_INVALID_ARGUMENT;
         BW_TRY(validate_cfg(ctx, v, cfg));
         reps |= kPrReps[v];
-        if (v == PR_PULL_SEGMENTED) need_split = true;
+        if (v == PR_PULL_SEGMENTED) need_inline = true;
         if (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV) need_exact = true;
         if (v == PR_VERTEX_PUSH || v == PR_VERTEX_PUSH_WARP || v == PR_VERTEX_PULL_WARP ||
             v == PR_VERTEX_PULL_WARP_NODIV)
@@ -1870,8 +2059,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     ctx->launches = 0;
     if (time_iterations) BW_TRY(ensure_level_events(ctx, iterations + 1));
 
-    PrRun split_run, exact_run;
-    if (need_split) BW_TRY(build_segments(ctx, g, 1, split_run, s));
+    PrRun inline_run, exact_run;
+    if (need_inline) BW_TRY(build_segments(ctx, g, 1, inline_run, s));
     if (need_exact) BW_TRY(build_segments(ctx, g, 0, exact_run, s));
     // heavy-unit tiles of the push and warp-pull variants
     uint4 *heavy_q = nullptr;
@@ -1895,12 +2084,12 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.deg = ctx->pr_deg;
     a.acc = ctx->pr_acc;
     a.gat_e = g->rev_edges;
-    if (need_split || need_exact) {
+    if (need_inline || need_exact) {
         // hub cache entries per block: chunk_size when given, else the
         // default for the shape; never more than the block's share of
         // shared memory allows
         const int block = (cfg && cfg->block_size == PULL_NARROW) ? PULL_NARROW : PULL_WIDE;
-        const uint64_t per_sm = block == PULL_WIDE ? 1 : static_cast<uint64_t>(pull_min_blocks(block, need_exact));
+        const uint64_t per_sm = static_cast<uint64_t>(pull_min_blocks(block));
         const size_t fixed = pull_fixed_smem(block);
         const size_t share = std::min<size_t>(ctx->max_smem_optin, ctx->max_smem_per_sm / per_sm);
         const uint64_t room = share > fixed + 1024 ? (share - fixed - 1024) / sizeof(float) : 0;
@@ -1909,13 +2098,13 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.hub_count = static_cast<uint32_t>(std::min<uint64_t>(std::min<uint64_t>(n, room), want)) & ~3u;
         const int bytes = static_cast<int>(fixed + a.hub_count * sizeof(float));
         if (block == PULL_WIDE) {
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, false, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_INLINE, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         } else {
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, false, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_STAGED, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, LONG_STAGED, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_INLINE, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         }
     }
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
@@ -1943,7 +2132,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, s);
         if (rc != BW_OK) {
             free_relabel(rl, s);
-            free_run(split_run, s);
+            free_run(inline_run, s);
             free_run(exact_run, s);
             return rc;
         }
@@ -2009,7 +2198,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
                 a.contrib_out = contrib[j & 1];
             }
         }
-        const PrRun &items = v == PR_PULL_SEGMENTED ? split_run : exact_run;
+        const PrRun &items = v == PR_PULL_SEGMENTED ? inline_run : exact_run;
         a.work = items.work;
         a.long_count = items.long_count;
         a.vals = items.vals;
@@ -2056,7 +2245,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         BW_CUDA(cudaMemcpyAsync(&diffs_dev_last, ctx->pr_diffs + iterations - 1, sizeof(float),
                                 cudaMemcpyDeviceToHost, s));
     BW_CUDA(cudaStreamSynchronize(s));
-    free_run(split_run, s);
+    free_run(inline_run, s);
     free_run(exact_run, s);
     free_relabel(rl, s);
     if (heavy_q) cudaFreeAsync(heavy_q, s);

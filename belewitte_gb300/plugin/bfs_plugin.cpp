@@ -17,7 +17,7 @@ namespace {
 
 struct BfsRun {
     unsigned root = 0;
-    size_t warp = 32, chunk = 32;
+    size_t warp = 0, chunk = 0;        // -w / -c; 0: tuned, else the library's 32 / 32
     LoadedGraph graph;
     int32_t *levels = nullptr;
 
@@ -35,6 +35,14 @@ struct BfsRun {
     bw_launch_config cfg() const
     {
         return bw_launch_config{0, 0, static_cast<uint32_t>(warp), static_cast<uint32_t>(chunk)};
+    }
+    // The launch of `variant`: -w / -c when given, else the autotuner's
+    // configuration for this graph (ImplementationTemplate.hpp:431-436 fixes
+    // 32 / 32 instead)
+    bw_launch_config cfg_for(int variant) const
+    {
+        if (warp || chunk) return cfg();
+        return tuned_config("bfs", bw_bfs_variant_name(variant), graph.host);
     }
     void write(std::ofstream &out)
     {
@@ -81,7 +89,7 @@ class BfsImplementation : public ImplementationBase {
         run_.alloc(n);
         Timer comp("computation");
         std::vector<bw_bfs_level_stats> stats(std::min<uint64_t>(n + 1, 1u << 20));
-        bw_launch_config cfg = run_.cfg();
+        bw_launch_config cfg = run_.cfg_for(variant_);
         for (size_t i = 0; i < run_count; i++) {
             bw_bfs_result res{};
             comp.start();
@@ -143,7 +151,7 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
         if (run_.root >= n) return;
         run_.alloc(n);
         Timer comp("computation");
-        bw_launch_config cfg = run_.cfg();
+        bw_launch_config cfg{};
         for (size_t i = 0; i < run_count; i++) {
             check_bw(bw_bfs_init(shared_context(), n, run_.root, run_.levels, nullptr), "bfs init");
             comp.start();
@@ -155,6 +163,7 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
             *depth_ = 0;
             set_frontier_stats(-1);
             int variant = predict_initial();
+            cfg = picked_config(run_.cfg_for(variant), is_warp(variant));
             uint32_t frontier = 1;
             int32_t depth = 0;
             do {
@@ -175,12 +184,21 @@ class BfsSwitch : public ImplementationBase, public SwitchBase {
                     *depth_ = depth;
                     set_frontier_stats(depth - 1);
                     int next = predict();
-                    if (next >= 0) variant = next;
+                    if (next >= 0) {
+                        variant = next;
+                        cfg = picked_config(run_.cfg_for(variant), is_warp(variant));
+                    }
                 }
             } while (frontier);
             comp.stop();
         }
         run_.write(out);
+    }
+
+    static bool is_warp(int variant)
+    {
+        const std::string name = bw_bfs_variant_name(variant);
+        return name.rfind("vertex-push-warp", 0) == 0 || name.rfind("vertex-pull-warp", 0) == 0;
     }
 
     // Statistics of the frontier the level at `depth` found (-1: {root}).

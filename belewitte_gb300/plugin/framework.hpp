@@ -184,6 +184,14 @@ struct LoadedGraph {
     ~LoadedGraph() { free(); }
 };
 
+// The autotuner's launch configuration for `variant` of `algorithm` ("bfs"
+// or "pagerank") on graph `g`: the entry for the graph's shape class (log2
+// of the vertex count, of the average degree and of the out-degree skew) in
+// data/autotune.tsv beside this framework's module, or of the nearest class
+// at most two steps away; all zero (the library default) when there is
+// none.  The environment variable BELEWITTE_AUTOTUNE names another file.
+bw_launch_config tuned_config(const std::string &algorithm, const std::string &variant, const bw_host_graph &g);
+
 void check_bw(int status, const std::string &what);
 bw_context *shared_context();   // one context per process (device chosen by kernel-runner)
 void set_device(int device);

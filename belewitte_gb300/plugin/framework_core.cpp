@@ -1,8 +1,13 @@
 // Framework implementation (linked into kernel-runner and exported to the
 // plugin libraries).  See framework.hpp for the reference correspondence.
+#include <dlfcn.h>
+
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <iomanip>
 #include <sstream>
 
@@ -24,6 +29,58 @@ void check_bw(int status, const std::string &what)
         std::string detail = status == BW_ERR_CUDA ? std::string(" [") + bw_last_error() + "]" : "";
         reportError(what + ": " + bw_status_string(status) + detail);
     }
+}
+
+// ----------------------------- tuned launches ------------------------------
+namespace {
+
+std::string tuned_file()
+{
+    if (const char *env = std::getenv("BELEWITTE_AUTOTUNE")) return env;
+    Dl_info info{};
+    if (!dladdr(reinterpret_cast<void *>(&tuned_config), &info) || !info.dli_fname) return "";
+    std::string path = info.dli_fname;
+    const size_t slash = path.rfind('/');
+    return (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/data/autotune.tsv";
+}
+
+// shape class fields: floor(log2(max(n, 2))), floor(log2(average degree, at
+// least 1)), floor(log2(max(max out-degree / average degree, 1)))
+std::array<int, 3> shape_class(const bw_host_graph &g)
+{
+    const double n = static_cast<double>(g.vertex_count), m = static_cast<double>(g.edge_count);
+    const double avg = std::max(m / std::max(n, 1.0), 1.0);
+    uint32_t dmax = 0;
+    for (uint64_t v = 0; g.fwd_vertices && v < g.vertex_count; v++)
+        dmax = std::max(dmax, g.fwd_vertices[v + 1] - g.fwd_vertices[v]);
+    return {static_cast<int>(std::floor(std::log2(std::max(n, 2.0)))), static_cast<int>(std::floor(std::log2(avg))),
+            static_cast<int>(std::floor(std::log2(std::max(static_cast<double>(dmax) / avg, 1.0))))};
+}
+
+}  // namespace
+
+bw_launch_config tuned_config(const std::string &algorithm, const std::string &variant, const bw_host_graph &g)
+{
+    bw_launch_config best{};
+    std::ifstream in(tuned_file());
+    if (!in) return best;
+    const std::array<int, 3> cls = shape_class(g);
+    int best_dist = 3;                      // farther classes keep the default
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream fields(line);
+        std::string algo, name, klass;
+        uint32_t b = 0, gr = 0, w = 0, c = 0;
+        if (!(fields >> algo >> name >> klass >> b >> gr >> w >> c) || algo != algorithm || name != variant) continue;
+        int v = 0, d = 0, k = 0;
+        if (std::sscanf(klass.c_str(), "v%d-d%d-s%d", &v, &d, &k) != 3) continue;
+        const int dist = std::abs(v - cls[0]) + std::abs(d - cls[1]) + std::abs(k - cls[2]);
+        if (dist < best_dist) {
+            best_dist = dist;
+            best = bw_launch_config{b, gr, w, c, 0};
+        }
+    }
+    return best;
 }
 
 static int g_device = 0;

@@ -66,6 +66,14 @@ class PageRankBase : public ImplementationBase {
         after_load();
     }
     virtual void after_load() {}
+    // The launch configuration of `variant`: the -w/-c options when given,
+    // else the autotuner's configuration for this graph
+    // (ImplementationTemplate.hpp:431-436 fixes 32 / 32 instead).
+    virtual bw_launch_config config_for(int variant)
+    {
+        if (warp_ || chunk_) return bw_launch_config{0, 0, static_cast<uint32_t>(warp_), static_cast<uint32_t>(chunk_)};
+        return tuned_config("pagerank", bw_pagerank_variant_name(variant), graph_.host);
+    }
     void freeGraph() override
     {
         if (ranks_) cudaFree(ranks_);
@@ -77,9 +85,9 @@ class PageRankBase : public ImplementationBase {
         const uint64_t n = graph_.view.vertex_count;
         if (cudaMalloc(reinterpret_cast<void **>(&ranks_), n * 4) != cudaSuccess) reportError("cudaMalloc failed");
         Timer comp("computation"), step("0:computation");
-        bw_launch_config cfg{0, 0, static_cast<uint32_t>(warp_), static_cast<uint32_t>(chunk_)};
         for (size_t i = 0; i < run_count; i++) {
             const int variant = pick();
+            const bw_launch_config cfg = config_for(variant);
             bw_pagerank_result res{};
             comp.start();
             check_bw(bw_pagerank_run(shared_context(), &graph_.view, variant, iterations_, ranks_, &cfg, 0, &res,
@@ -98,7 +106,7 @@ class PageRankBase : public ImplementationBase {
     }
 
     unsigned iterations_ = 100;
-    size_t warp_ = 32, chunk_ = 32;
+    size_t warp_ = 0, chunk_ = 0;      // -w / -c; 0: tuned, else the library's 32 / 32
     int reps_ = 63;
     LoadedGraph graph_;
     float *ranks_ = nullptr;
@@ -159,6 +167,12 @@ class PageRankSwitch : public PageRankBase, public SwitchBase {
     }
     prop_ref *log_sum_, *log_sq_sum_, *log_max_;
     void runImplementation(std::ofstream &out) override { run(out, [this] { return predict_initial(); }); }
+    // a warp variant runs with the warp and chunk sizes its predictor slot gives
+    bw_launch_config config_for(int variant) override
+    {
+        const bool warp = std::string(bw_pagerank_variant_name(variant)).find("-warp") != std::string::npos;
+        return picked_config(PageRankBase::config_for(variant), warp);
+    }
 };
 
 }  // namespace

@@ -91,6 +91,8 @@ class SwitchBase {
             }
             impls_.resize(names.size());
             ids_.resize(names.size());
+            warp_.assign(names.size(), 0);
+            chunk_.assign(names.size(), 0);
             for (auto &t : names) {
                 const size_t idx = std::get<2>(t);
                 const int v = lookup_variant(std::get<0>(t));
@@ -101,6 +103,10 @@ class SwitchBase {
                 }
                 impls_[idx] = v;
                 ids_[idx] = std::get<1>(t);
+                // the warp and chunk sizes the slot runs its warp kernels
+                // with (ImplementationTemplate.hpp:806-816: setWarpConfig)
+                warp_[idx] = static_cast<uint32_t>(std::get<3>(t));
+                chunk_[idx] = static_cast<uint32_t>(std::get<4>(t));
             }
             if (missing) reportError("Missing properties/implementations!");
             for (auto &p : props) bound_.insert(p.first);
@@ -109,6 +115,8 @@ class SwitchBase {
             default_ = 0;
             impls_.push_back(lookup_variant(default_name));
             ids_.push_back(-1);
+            warp_.assign(1, 0);
+            chunk_.assign(1, 0);
         }
         for (auto *table : {&graph_props_, &algo_props_})
             for (auto &p : *table)
@@ -142,6 +150,22 @@ class SwitchBase {
             return impls_[static_cast<size_t>(r)];
         }
         return -1;
+    }
+
+    // The launch configuration of the implementation picked last: `base`
+    // (the -w/-c options) with, for a warp variant, the warp and chunk sizes
+    // the predictor's implNames entry gives it, as the reference applies
+    // them to its warp kernels (setWarpConfig, ImplementationTemplate.hpp:
+    // 806-816).  Logged as "config:<step>:<warp>:<chunk>".
+    bw_launch_config picked_config(bw_launch_config base, bool warp_variant)
+    {
+        if (!warp_variant || !lookup_ || last_ < 0) return base;
+        const uint32_t w = warp_[static_cast<size_t>(last_)], c = chunk_[static_cast<size_t>(last_)];
+        if (w == 0 || c == 0) return base;
+        base.warp_size = w;
+        base.chunk_size = c;
+        if (log_.is_open()) log_ << "config:" << step_ << ":" << w << ":" << c << "\n";
+        return base;
     }
 
     void close()
@@ -183,6 +207,7 @@ class SwitchBase {
     size_t step_ = 0;
     std::vector<int> impls_;
     std::vector<int64_t> ids_;
+    std::vector<uint32_t> warp_, chunk_;       // implNames fields 3 and 4 per slot
     std::set<std::string> bound_;              // properties the predictor owns
     std::map<std::string, double> storage_;    // the others (map nodes do not move)
     std::ofstream log_;

@@ -196,6 +196,7 @@ int bw_graph_file_write(const char *path, const bw_host_graph *g);
  */
 int bw_degree_statistics(const bw_host_graph *g, int kind, double out[7]);
 
+
 /* ------------------------------------------------------------------------ */
 /* Context                                                                   */
 /* ------------------------------------------------------------------------ */
@@ -250,6 +251,19 @@ int bw_expand_edge_list(const uint32_t *vertices, uint64_t vertex_count,
 int bw_build_struct_edges(const uint32_t *in_edges, const uint32_t *out_edges,
                           uint64_t edge_count, uint32_t *struct_edges,
                           void *stream);
+
+
+/*
+ * The same statistics of a device-resident graph, computed on the device
+ * (graph-details.cpp:36-61 over a graph already loaded for the kernels):
+ * degrees from the view's offsets (fwd_vertices for out, rev_vertices for
+ * in; abs adds both, or takes out only when `undirected`), sorted on the
+ * device for the order statistics; mean and standard deviation from exact
+ * integer sums of d and d^2 (the host's Welford loop agrees to ~1e-12).
+ * Synchronises `stream` to return the figures.
+ */
+int bw_degree_statistics_device(bw_context *ctx, const bw_graph_view *g, int undirected, int kind,
+                                double out[7], void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* BFS                                                                       */

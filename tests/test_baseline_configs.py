@@ -107,7 +107,7 @@ def test_config1_reference_kernels(config1):
 # ------------------------------------------------- config 2 (full sizes)
 def _pagerank_full_size(ctx, kind, kw):
     import torch
-    g = bw.DeviceGraph.generate(kind, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR, **kw)
+    g = bw.DeviceGraph.generate(kind, reps=63, **kw)
     host = g.to_host_arrays()
     n = g.vertex_count
     deg = np.diff(host["fwd_vertices"].astype(np.int64)).astype(np.uint32)
@@ -156,7 +156,7 @@ def test_config3_bfs_sources(ctx, kind, kw):
     oracle's queue BFS."""
     import torch
     from belewitte_gb300 import learn
-    g = bw.DeviceGraph.generate(kind, reps=bw.REP_FWD_CSR | bw.REP_REV_CSR, **kw)
+    g = bw.DeviceGraph.generate(kind, reps=63, **kw)
     host = g.to_host_arrays()
     n = g.vertex_count
     hub = int(np.argmax(np.diff(host["fwd_vertices"].astype(np.int64))))

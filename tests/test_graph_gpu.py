@@ -33,3 +33,31 @@ def test_device_generator_equals_host_generator(kind, kw, host):
     got = g.to_host_arrays()
     for k in ("fwd_vertices", "fwd_edges", "rev_vertices", "rev_edges"):
         assert np.array_equal(got[k], getattr(h, k)), (kind, k)
+
+
+@pytest.mark.parametrize("name", ["rmat14", "rmat12_sym", "er", "grid", "ba", "star", "tiny", "isolated", "chain"])
+def test_device_degree_statistics_equal_host(ctx, name):
+    """graph-details statistics on the device equal the host restatement:
+    the order statistics and the mean exactly, the standard deviation to
+    1e-12 (exact integer sums on the device, a Welford loop on the host)."""
+    from tests.graphs import catalog
+    h = catalog()[name][0]()
+    g = bw.DeviceGraph(h)
+    for kind in ("abs", "in", "out"):
+        want = h.degree_statistics(kind)
+        got = g.degree_statistics(ctx, kind)
+        for k in ("min", "lower", "mean", "median", "upper", "max"):
+            assert got[k] == want[k], (name, kind, k)
+        assert got["stddev"] == pytest.approx(want["stddev"], rel=1e-12, abs=1e-12), (name, kind)
+
+
+def test_device_degree_statistics_at_scale(ctx):
+    """R-MAT scale 22 (the headline graph), generated on the device."""
+    h = bw.HostGraph.rmat(20, 16, seed=22)
+    g = bw.DeviceGraph.generate("rmat", scale=20, edge_factor=16, seed=22)
+    for kind in ("abs", "in", "out"):
+        want = h.degree_statistics(kind)
+        got = g.degree_statistics(ctx, kind)
+        assert [got[k] for k in ("min", "lower", "mean", "median", "upper", "max")] == \
+            [want[k] for k in ("min", "lower", "mean", "median", "upper", "max")]
+        assert got["stddev"] == pytest.approx(want["stddev"], rel=1e-12)

@@ -129,6 +129,22 @@ def test_device_and_host_predictions_agree(ctx):
     assert [s["variant"] for s in a.level_stats] == [s["variant"] for s in b.level_stats]
 
 
+def test_learned_schedule_is_deterministic(ctx):
+    """The level statistics are summed in fixed point, so every run on the
+    same graph and root sees the same features and picks the same variant
+    for every level, whichever order the threads added in."""
+    pred = learn.load_predictor()
+    for h in (bw.HostGraph.rmat(16, 16, seed=4, symmetrise=True), bw.HostGraph.barabasi_albert(60000, 4, seed=2)):
+        g = bw.DeviceGraph(h)
+        r = h.max_out_degree_vertex()
+        runs = [learn.run_learned(ctx, g, pred, r, loop=loop) for loop in ("graph", "graph", "host", "host")]
+        first = runs[0].level_stats
+        for run in runs[1:]:
+            assert [s["variant"] for s in run.level_stats] == [s["variant"] for s in first]
+            assert [(s["log_degree_sum"], s["log_degree_sq_sum"]) for s in run.level_stats] == \
+                [(s["log_degree_sum"], s["log_degree_sq_sum"]) for s in first]
+
+
 def test_cluster_sized_frontiers_run_frontier_push(ctx):
     """The device loop gives every level whose frontier the cluster kernel
     takes to frontier-push, and the MLP the rest; depths are unchanged."""

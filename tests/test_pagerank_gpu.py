@@ -1,11 +1,14 @@
 """PageRank parity on the GPU through the C ABI, every variant.
 
 Tolerances (stated by the requirement this library is built to):
-  * vertex-pull, vertex-pull-nodiv: bit-exact against the oracle (same
-    sequential row order and the same float / double operations);
-  * every other variant: max relative error <= 1e-5 against the oracle of
-    its semantics class (their float atomics / warp reductions reorder the
-    sum), and <= 1e-4 against the FP64 oracle.
+  * vertex-pull, vertex-pull-nodiv, pull-segmented: bit-exact against the
+    oracle (the reference's sequential row order and the same float /
+    double operations);
+  * the float-atomic variants (edge lists, push, warp pull -- the reference's
+    own kernels of these names add with float atomics in no fixed order):
+    max relative error <= 1e-5 against the oracle of their semantics class
+    where the reference's own sum is that close to exact, and <= 1e-4
+    against the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -19,7 +22,7 @@ pytestmark = pytest.mark.gpu
 REL_REF = 1e-5
 REL_F64 = 1e-4
 GRAPHS = ["rmat10", "rmat12_sym", "rmat14", "er", "grid", "ba", "chain", "star", "tiny", "isolated"]
-BITEXACT = {"vertex-pull", "vertex-pull-nodiv"}
+BITEXACT = {"vertex-pull", "vertex-pull-nodiv", "pull-segmented"}
 
 
 @pytest.fixture(scope="module")
@@ -100,21 +103,14 @@ def test_long_rows(ctx, long_graphs, variant, iterations):
     variants take (batches of rows up to 2048 terms summed one row per lane,
     longer rows summed piece-parallel), including a 199,999-term row of
     equal terms (a round-half-even tie at nearly every step), rows at every
-    length boundary and R-MAT hubs: bit-identical to the reference.  The
-    reference's own loop can be far from FP64 on such rows (1.2e-3 after one
-    iteration on the equal-term row), so pull-segmented, which reorders the
-    sum, is held to the reference only where the reference is within 1e-5
-    of FP64, and to FP64 everywhere."""
+    length boundary and R-MAT hubs: bit-identical to the reference (whose
+    own loop is 1.2e-3 from FP64 after one iteration on the equal-term
+    row)."""
     for kind, (h, g) in long_graphs.items():
         got = bw.pagerank(ctx, g, variant, iterations).ranks.cpu().numpy()
         div, nodiv, d64, n64 = _oracles(h, iterations)
-        ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
-        if variant in BITEXACT:
-            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, kind)
-            continue
-        if _rel(ref, r64) <= REL_REF:
-            assert _rel(got, ref) <= REL_REF, (variant, kind)
-        assert _rel(got, r64) <= REL_F64, (variant, kind)
+        ref = nodiv if "nodiv" in variant else div
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, kind)
 
 
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
@@ -128,11 +124,8 @@ def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs, relabel):
     for name, (h, g) in list(long_graphs.items()) + [("rmat14", graphs["rmat14"]), ("chain", graphs["chain"])]:
         got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs, relabel=relabel).ranks.cpu().numpy()
         div, nodiv, d64, n64 = _oracles(h, 30)
-        ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
-        if variant in BITEXACT:
-            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name, block, hubs)
-        elif _rel(ref, r64) <= REL_REF:
-            assert _rel(got, ref) <= REL_REF, (variant, name, block, hubs)
+        ref = nodiv if "nodiv" in variant else div
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name, block, hubs)
 
 
 @pytest.mark.parametrize("variant", ["vertex-push-warp", "vertex-pull-warp", "vertex-pull-warp-nodiv"])
@@ -200,8 +193,14 @@ def test_reverse_only_view(ctx, graphs, long_graphs, variant):
         ref, r64 = (nodiv, n64) if "nodiv" in variant else (div, d64)
         if variant in BITEXACT:
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name)
-        elif _rel(ref, r64) <= REL_REF:
-            assert _rel(got, ref) <= REL_REF, (variant, name)
+        else:
+            # vertex-pull-warp: the reference's kernel adds its lanes' partial
+            # sums with float atomics, so its order is unspecified; held to
+            # the oracle where the reference's own sum is within 1e-5 of
+            # exact, and to FP64 everywhere
+            if _rel(ref, r64) <= REL_REF:
+                assert _rel(got, ref) <= REL_REF, (variant, name)
+            assert _rel(got, r64) <= REL_F64, (variant, name)
 
 
 def test_gather_probe(ctx):

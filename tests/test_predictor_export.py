@@ -194,7 +194,9 @@ def test_kernel_runner_pagerank_switch_with_exported_predictor(predictor_so, tmp
         assert pred.candidates[preds[0]] == sched[1], (name, pred.candidates[preds[0]], sched)
         ref, _ = oracle.pagerank(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 30)
         got = np.loadtxt(tmp_path / f"{name}.output", dtype=np.float64)[:, 1]
-        assert float((np.abs(got - ref) / np.abs(ref)).max()) <= 2e-5, name
+        # the schedule may pick float-atomic variants (<= 1e-5 from the
+        # reference); the --validate output rounds to 7 significant digits
+        assert float((np.abs(got - ref) / np.abs(ref)).max()) <= 1e-5 + 5e-7, name
 
 
 def ctx_of():
