@@ -380,6 +380,9 @@ class PageRankRun:
     kernel_launches: int = 0  # this library's kernels the run launched
 
 
+L2_WINDOW = 4      # BW_LAUNCH_L2_WINDOW
+
+
 def _relabel_flags(relabel):
     """None: the library decides; True / False force the hub-first order."""
     return 0 if relabel is None else (_abi.LAUNCH_RELABEL if relabel else _abi.LAUNCH_NO_RELABEL)
@@ -414,7 +417,8 @@ def _tuned(algorithm: str, variant, g, block, grid, warp, chunk, tuned: bool):
 
 def bfs(ctx: Context, g: DeviceGraph, variant: str | int, root: int, *, levels=None,
         loop: str = "host", max_levels: int = 0, stats: bool = False, block: int = 0,
-        grid: int = 0, warp: int = 0, chunk: int = 0, tuned: bool = True, stream=None) -> BfsRun:
+        grid: int = 0, warp: int = 0, chunk: int = 0, tuned: bool = True, l2_window: bool = False,
+        stream=None) -> BfsRun:
     """BFS from `root` with a fixed variant (BFS::runImplementation).  With
     no geometry given, the autotuner's configuration for the graph's shape
     class is used (tuned=False: the library default)."""
@@ -429,7 +433,8 @@ def bfs(ctx: Context, g: DeviceGraph, variant: str | int, root: int, *, levels=N
     cap = min(cap, 1 << 20)
     arr = (_abi.BfsLevelStats * cap)() if cap else None
     rc = lib.bw_bfs_run(ctx.handle, C.byref(g.view), bfs_variant_id(variant), root, _ptr(levels),
-                        C.byref(_cfg(block, grid, warp, chunk)), 1 if loop == "graph" else 0,
+                        C.byref(_cfg(block, grid, warp, chunk, L2_WINDOW if l2_window else 0)),
+                        1 if loop == "graph" else 0,
                         max_levels, C.byref(res), arr, cap, C.c_void_p(st.cuda_stream))
     check(rc, f"bfs {variant}")
     run = BfsRun(levels, res.level_count, res.visited, res.traversed_edges, res.device_ms)
@@ -463,7 +468,8 @@ def bfs_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], ro
 
 def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int = 30, *,
              ranks=None, block: int = 0, grid: int = 0, warp: int = 0, chunk: int = 0,
-             relabel: bool | None = None, loop: str = "host", tuned: bool = True, stream=None) -> PageRankRun:
+             relabel: bool | None = None, loop: str = "host", tuned: bool = True, l2_window: bool = False,
+             stream=None) -> PageRankRun:
     """PageRank, damping 0.85, 1/N init, exactly `iterations` iterations.
     With no geometry given, the autotuner's configuration for the graph's
     shape class is used (tuned=False: the library default)."""
@@ -476,7 +482,8 @@ def pagerank(ctx: Context, g: DeviceGraph, variant: str | int, iterations: int =
     res = _abi.PagerankResult()
     diffs = (C.c_float * max(iterations, 1))()
     rc = lib.bw_pagerank_run(ctx.handle, C.byref(g.view), pagerank_variant_id(variant), iterations,
-                             _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk, _relabel_flags(relabel))),
+                             _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk,
+                                                       _relabel_flags(relabel) | (L2_WINDOW if l2_window else 0))),
                              1 if loop == "graph" else 0, C.byref(res), diffs, C.c_void_p(st.cuda_stream))
     check(rc, f"pagerank {variant}")
     return PageRankRun(ranks, res.iterations, res.device_ms, list(diffs)[:iterations],
@@ -528,10 +535,16 @@ def gather_probe_sum(ctx: Context, src, idx, stream=None) -> float:
 
 def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int], iterations: int = 30,
                       *, ranks=None, time_iterations: bool = False, block: int = 0, grid: int = 0,
-                      warp: int = 0, chunk: int = 0, relabel: bool | None = None, stream=None) -> PageRankRun:
+                      warp: int = 0, chunk: int = 0, relabel: bool | None = None, tuned: bool = True,
+                      l2_window: bool = False, stream=None) -> PageRankRun:
+    """PageRank with a per-iteration variant schedule (last entry repeats).
+    A one-variant schedule with no geometry given runs the autotuner's
+    configuration, as pagerank() does."""
     torch = _torch()
     lib = library()
     sched = [pagerank_variant_id(v) for v in schedule]
+    if len(set(sched)) == 1:
+        block, grid, warp, chunk = _tuned("pagerank", sched[0], g, block, grid, warp, chunk, tuned)
     arr_s = (C.c_int32 * len(sched))(*sched)
     if ranks is None:
         ranks = torch.empty(g.vertex_count, dtype=torch.float32, device=f"cuda:{ctx.device}")
@@ -540,7 +553,8 @@ def pagerank_schedule(ctx: Context, g: DeviceGraph, schedule: Iterable[str | int
     it_ms = (C.c_float * max(iterations, 1))()
     rc = lib.bw_pagerank_run_schedule(ctx.handle, C.byref(g.view), arr_s, len(sched), iterations,
                                       _ptr(ranks), C.byref(_cfg(block, grid, warp, chunk,
-                                                                _relabel_flags(relabel))),
+                                                                _relabel_flags(relabel) |
+                                                                (L2_WINDOW if l2_window else 0))),
                                       int(time_iterations), it_ms, C.byref(res), C.c_void_p(st.cuda_stream))
     check(rc, "pagerank schedule")
     run = PageRankRun(ranks, res.iterations, res.device_ms, kernel_launches=res.kernel_launches)

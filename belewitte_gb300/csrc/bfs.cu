@@ -364,6 +364,14 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
         cudaStream_t cap;
         e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
         if (e != cudaSuccess) { fail(e, "cudaStreamCreate"); break; }
+        // BW_LAUNCH_L2_WINDOW: the captured kernels keep the depth array persisting in L2
+        L2Window win_cap;
+        if (cfg && (cfg->flags & BW_LAUNCH_L2_WINDOW) &&
+            l2_window_begin(ctx, cap, levels, n * sizeof(int32_t), win_cap, false) != BW_OK) {
+            cudaStreamDestroy(cap);
+            rc = BW_ERR_CUDA;
+            break;
+        }
         e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
             BfsArgs a = make_args(ctx, g, levels, -1, cfg);
@@ -383,6 +391,7 @@ int run_graph(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t roo
         } else {
             fail(e, "cudaStreamBeginCaptureToGraph");
         }
+        l2_window_end(win_cap);                 // before its stream goes
         cudaStreamDestroy(cap);
         if (rc) break;
         e = cudaGraphInstantiate(&exec, graph, 0);
@@ -570,6 +579,9 @@ int bw_bfs_run(bw_context *ctx, const bw_graph_view *g, int variant, uint32_t ro
     if (loop_mode != BW_LOOP_GRAPH && loop_mode != BW_LOOP_HOST) return BW_ERR_INVALID_ARGUMENT;
     if (g && g->edge_count == 0) return bfs_edgeless(ctx, g, variant, root, levels, result, stats, stats_capacity, s);
     BW_TRY(prepare(ctx, g, reps, side, levels, root, s));
+    L2Window win;                  // BW_LAUNCH_L2_WINDOW: the depth array persisting in L2
+    if (cfg && (cfg->flags & BW_LAUNCH_L2_WINDOW))
+        BW_TRY(l2_window_begin(ctx, s, levels, g->vertex_count * sizeof(int32_t), win));
     if (loop_mode == BW_LOOP_GRAPH)
         return run_graph(ctx, g, variant, root, levels, cfg, max_levels, side, result, stats, stats_capacity, s);
     if (loop_mode != BW_LOOP_HOST) return BW_ERR_INVALID_ARGUMENT;

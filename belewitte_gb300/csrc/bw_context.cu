@@ -1,3 +1,4 @@
+#include <algorithm>
 // Context, scratch management, launch geometry and representation builders.
 #include <cstdio>
 #include <cstring>
@@ -100,8 +101,10 @@ int ensure_pr_scratch(bw_context *ctx, uint64_t n, uint32_t iterations)
 {
     if (n > ctx->pr_n_cap) {
         BW_TRY(grow(&ctx->pr_acc, n));
-        BW_TRY(grow(&ctx->pr_buf[0], n));
-        BW_TRY(grow(&ctx->pr_buf[1], n));
+        // both contribution buffers in one allocation, so one L2
+        // access-policy window covers the vector every iteration gathers
+        BW_TRY(grow(&ctx->pr_buf[0], 2 * n));
+        ctx->pr_buf[1] = ctx->pr_buf[0] + n;
         BW_TRY(grow(&ctx->pr_deg, n));
         ctx->pr_n_cap = n;
     }
@@ -235,8 +238,7 @@ int bw_context_destroy(bw_context *ctx)
     cudaFree(ctx->heavy);
     cudaFree(ctx->outdeg);
     cudaFree(ctx->pr_acc);
-    cudaFree(ctx->pr_buf[0]);
-    cudaFree(ctx->pr_buf[1]);
+    cudaFree(ctx->pr_buf[0]);                 // pr_buf[1] lies inside it
     cudaFree(ctx->pr_deg);
     cudaFree(ctx->pr_diffs);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -287,3 +289,57 @@ int bw_build_struct_edges(const uint32_t *in_edges, const uint32_t *out_edges,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// L2 access-policy window (BW_LAUNCH_L2_WINDOW)
+// ---------------------------------------------------------------------------
+namespace bw {
+
+L2Window::~L2Window() { l2_window_end(*this); }
+
+int l2_window_begin(bw_context *ctx, cudaStream_t s, const void *base, size_t bytes, L2Window &w, bool carve_out)
+{
+    l2_window_end(w);
+    if (!base || bytes == 0) return BW_OK;
+    // a window is a stream attribute: the legacy default stream (and the
+    // per-thread one) carries none
+    if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+        set_last_error(cudaErrorInvalidResourceHandle, "BW_LAUNCH_L2_WINDOW needs a created stream");
+        return BW_ERR_INVALID_ARGUMENT;
+    }
+    int persist_max = 0, window_max = 0;
+    BW_CUDA(cudaDeviceGetAttribute(&persist_max, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
+    BW_CUDA(cudaDeviceGetAttribute(&window_max, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
+    if (persist_max <= 0 || window_max <= 0) return BW_OK;      // not supported: nothing to do
+    const size_t span = std::min<size_t>(bytes, static_cast<size_t>(window_max));
+    const size_t carve = std::min<size_t>(span, static_cast<size_t>(persist_max));
+    if (carve_out) BW_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, carve));
+    w.carved = carve_out;
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.base_ptr = const_cast<void *>(base);
+    v.accessPolicyWindow.num_bytes = span;
+    v.accessPolicyWindow.hitRatio = static_cast<float>(std::min(1.0, static_cast<double>(carve) / span));
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    BW_CUDA(cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &v));
+    w.stream = s;
+    w.on = true;
+    w.bytes = span;
+    return BW_OK;
+}
+
+void l2_window_end(L2Window &w)
+{
+    if (!w.on) return;
+    cudaStreamAttrValue v{};                       // an empty window
+    v.accessPolicyWindow.num_bytes = 0;
+    cudaStreamSetAttribute(w.stream, cudaStreamAttributeAccessPolicyWindow, &v);
+    if (w.carved) {
+        cudaCtxResetPersistingL2Cache();           // the lines go back to normal
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
+    w.on = false;
+    w.carved = false;
+}
+
+}  // namespace bw

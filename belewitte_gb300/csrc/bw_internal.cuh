@@ -171,6 +171,28 @@ int ensure_level_events(bw_context *ctx, uint32_t count);
 
 inline cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
 
+// BW_LAUNCH_L2_WINDOW: an access-policy window that keeps [base, base +
+// bytes) persisting in L2 for the kernels of `s` (and of graphs captured
+// from it), with a persisting carve-out of the same size (at most the
+// device's maximum); l2_window_end removes the window, resets the
+// persisting lines and the carve-out to 0.  A context-level setting: it
+// ends with the process.
+struct L2Window {
+    cudaStream_t stream = nullptr;
+    bool on = false;
+    bool carved = false;                           // this window set the carve-out
+    size_t bytes = 0;
+    L2Window() = default;
+    L2Window(const L2Window &) = delete;
+    L2Window &operator=(const L2Window &) = delete;
+    ~L2Window();                                   // l2_window_end
+};
+// carve_out false: the window only (a stream whose kernels run under a
+// carve-out another window holds, e.g. one that captures a graph).
+int l2_window_begin(bw_context *ctx, cudaStream_t s, const void *base, size_t bytes, L2Window &w,
+                    bool carve_out = true);
+void l2_window_end(L2Window &w);
+
 // Persistent-style default grid: `per_sm` blocks per SM.
 inline unsigned default_grid(const bw_context *ctx, unsigned per_sm)
 { return static_cast<unsigned>(ctx->sm_count) * per_sm; }

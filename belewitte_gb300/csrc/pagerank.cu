@@ -103,6 +103,7 @@ struct PrArgs {
     // Decided on the device, so the host never waits inside a run:
     const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
+    const uint32_t *piece_total;  // device: long-row pieces at the head of the list
     const float *gat_in;
     float *gat_out;
     double base_div;           // (1.0 - 0.85f) / N, computed once on the host
@@ -1364,18 +1365,34 @@ __device__ __forceinline__ float gather_padded(const uint32_t *__restrict__ ge, 
     return part;
 }
 
-template<bool NODIV>
-__device__ __noinline__ void inline_piece(const PrArgs &a, uint32_t item, uint32_t row, uint32_t e0, uint32_t e1,
-                                             const float *src, const float *hub, uint32_t hubs, float *buf,
-                                             unsigned lane, float base_nd, float &dsum)
+// What inline_piece needs of the kernel's arguments (passed apart from
+// PrArgs, so that the kernel keeps its own copy in registers).
+struct PieceIo {
+    const uint32_t *rev_v;        // reverse-CSR offsets
+    const uint32_t *ge;           // gathered-array positions of the sources
+    const float *src;             // the gathered array
+    const float *hub;             // its first `hubs` entries, in shared memory
+    uint32_t hubs;
+    uint32_t *psum;               // posted piece sums (PSUM_EMPTY: none yet)
+    uint4 *rec;                   // piece records, two uint4 each
+    uint32_t *arrivals;           // per-row arrival counters
+};
+
+// One piece of a long row; true (in every lane) when this warp summed the
+// whole row: *total is then the row's sequential sum, for the caller to
+// consolidate.
+__device__ __forceinline__ bool inline_piece(const PieceIo io, uint32_t item, uint32_t row, uint32_t e0, uint32_t e1,
+                                          float *buf, unsigned lane, float *total)
 {
     using namespace bwseq;
-    const uint32_t *ge = a.gat_e;
-    const uint32_t rb = a.rev_v[row], n = a.rev_v[row + 1] - rb;
+    const uint32_t *ge = io.ge;
+    const float *src = io.src, *hub = io.hub;
+    const uint32_t hubs = io.hubs;
+    const uint32_t rb = io.rev_v[row], n = io.rev_v[row + 1] - rb;
     const uint32_t pieces = row_pieces(n, 1);
     const uint32_t q = e0 == rb ? 0u : 1u + (e0 - rb - SERIAL_TERMS) / SEG_EDGES;
     const uint32_t p0 = item - q;
-    uint32_t *psum = reinterpret_cast<uint32_t *>(a.piece_sum);
+    uint32_t *psum = io.psum;
     uint4 r0 = make_uint4(REC_NONE, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
     if (q == 0) {
         // the serial start, in row order by lane 0 (four terms per load)
@@ -1397,11 +1414,11 @@ __device__ __noinline__ void inline_piece(const PrArgs &a, uint32_t item, uint32
             }
             __syncwarp();
         }
-        if (pieces == 1) {
-            if (lane == 0) dsum += finish_vertex<NODIV>(a, row, acc, base_nd);
-            return;
-        }
         const uint32_t sb = __shfl_sync(FULL_MASK, __float_as_uint(acc), 0);
+        if (pieces == 1) {
+            *total = __uint_as_float(sb);
+            return true;
+        }
         if (lane == 0) st_release_u32(psum + item, sb);
         r0 = make_uint4(REC_STATE, sb, 0u, 0u);
     } else {
@@ -1438,14 +1455,14 @@ __device__ __noinline__ void inline_piece(const PrArgs &a, uint32_t item, uint32
     }
     uint32_t last = 0;
     if (lane == 0) {
-        a.piece_map[2 * static_cast<uint64_t>(item)] = r0;
-        a.piece_map[2 * static_cast<uint64_t>(item) + 1] = r1;
-        last = atomic_add_acq_rel(&a.long_count[row], 1u) + 1 == pieces ? 1u : 0u;
+        io.rec[2 * static_cast<uint64_t>(item)] = r0;
+        io.rec[2 * static_cast<uint64_t>(item) + 1] = r1;
+        last = atomic_add_acq_rel(&io.arrivals[row], 1u) + 1 == pieces ? 1u : 0u;
     }
-    if (!__shfl_sync(FULL_MASK, last, 0)) return;
+    if (!__shfl_sync(FULL_MASK, last, 0)) return false;
     __syncwarp();                                     // every lane's reads after lane 0's acquire
-    const float total = combine_records(
-        a.piece_map + 2 * static_cast<uint64_t>(p0), 1u, pieces, lane,
+    *total = combine_records(
+        io.rec + 2 * static_cast<uint64_t>(p0), 1u, pieces, lane,
         [&](uint32_t qq, uint32_t sb) {
             const uint32_t b = SERIAL_TERMS + (qq - 1) * SEG_EDGES;
             const bool ok = warp_sequential_continue_load<PIECE_L>(
@@ -1459,11 +1476,9 @@ __device__ __noinline__ void inline_piece(const PrArgs &a, uint32_t item, uint32
                 for (uint32_t i = 0; i < n; i++) t = __fadd_rn(t, gather1(src, hub, hubs, __ldcg(ge + rb + i)));
             return __shfl_sync(FULL_MASK, t, 0);
         });
-    if (lane == 0) {
-        dsum += finish_vertex<NODIV>(a, row, total, base_nd);
-        a.long_count[row] = 0;
-    }
+    if (lane == 0) io.arrivals[row] = 0;
     for (uint32_t i = lane; i < pieces; i += 32) psum[p0 + i] = PSUM_EMPTY;   // for the next iteration
+    return true;
 }
 
 // Long rows of the work-list kernel: staged in vals[] for k_pr_long_sums
@@ -1489,16 +1504,15 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
         reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
     __syncthreads();
     float dsum = 0.0f;
+    // inline: the long-row pieces at the head of the list are
+    // k_pr_long_pieces' work
+    const uint64_t first = MODE == LONG_INLINE ? *a.piece_total : 0u;
     // the next item's descriptor is loaded one item ahead
-    uint4 w_next = warp < a.work_count ? a.work[warp] : make_uint4(0, 0, 0, 0);
-    for (uint64_t it = warp; it < a.work_count; it += warps) {
+    uint4 w_next = first + warp < a.work_count ? a.work[first + warp] : make_uint4(0, 0, 0, 0);
+    for (uint64_t it = first + warp; it < a.work_count; it += warps) {
         const uint4 w = w_next;
         if (it + warps < a.work_count) w_next = a.work[it + warps];
         const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
-        if (MODE == LONG_INLINE && (w.y & LONG_FLAG)) {
-            inline_piece<NODIV>(a, static_cast<uint32_t>(it), r0, e0, e1, src, hub, hubs, buf, lane, base_nd, dsum);
-            continue;
-        }
         if (MODE == LONG_STAGED && (w.y & LONG_FLAG)) {
             // exact piece: store the gathered terms in edge order (the
             // long-row sums run in k_pr_long_sums after this kernel) and
@@ -1553,6 +1567,44 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
     }
     add_diff(a.diff, dsum);
 }
+
+// pull-segmented's long rows: the pieces at the head of the work list
+// (inline_piece), one warp per piece in list order -- a row's pieces are
+// neighbours, so they run in the same round -- before k_pr_pull_items takes
+// the short rows.  Its own kernel, so that each keeps its registers: 512
+// threads, a shared-memory copy of the first hub_count entries of the
+// gathered array like the work-list kernel's.
+constexpr int PIECE_THREADS = 512;
+
+template<bool NODIV>
+__global__ void __launch_bounds__(PIECE_THREADS, 1) k_pr_long_pieces(PrArgs a)
+{
+    constexpr int WARPS = PIECE_THREADS / 32;
+    resolve_args(a);
+    extern __shared__ __align__(16) float smem_f[];
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
+    float *buf = smem_f + wib * PULL_BUF;
+    float *hub = smem_f + WARPS * PULL_BUF;
+    const uint32_t hubs = a.hub_count;
+    for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
+        reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
+    __syncthreads();
+    const PieceIo io{a.rev_v, a.gat_e, src, hub, hubs, reinterpret_cast<uint32_t *>(a.piece_sum), a.piece_map,
+                     a.long_count};
+    const float base_nd = nodiv_base(a.n);
+    const uint64_t P = *a.piece_total;
+    float dsum = 0.0f;
+    for (uint64_t it = warp; it < P; it += warps) {
+        const uint4 w = a.work[it];
+        float total;
+        if (inline_piece(io, static_cast<uint32_t>(it), w.x, w.z, w.w, buf, lane, &total) && lane == 0)
+            dsum += finish_vertex<NODIV>(a, w.x, total, base_nd);
+    }
+    add_diff(a.diff, dsum);
+}
+constexpr size_t piece_smem() { return (PIECE_THREADS / 32) * PULL_BUF * sizeof(float); }
 
 // Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
 // after the iteration's work-list kernel has stored every long row's terms
@@ -1685,6 +1737,7 @@ struct PrRun {
     float *piece_sum = nullptr;        // exact pieces: their float sums
     uint4 *piece_map = nullptr;        // giant-row pieces: records (two uint4 each)
     uint32_t *sum_ctr = nullptr;       // k_pr_long_sums' job and finish counters
+    const uint32_t *piece_total = nullptr;     // device: pieces at the head of the list
     const uint32_t *count_all = nullptr;       // device: items in the list
     const uint32_t *count_nonconst = nullptr;  // device: items before the CONST ones
 };
@@ -1849,6 +1902,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int inl, PrRun &run,
     BW_CUDA(cudaGetLastError());
     run.count_nonconst = tot;
     run.count_all = tot + 1;
+    run.piece_total = ppos + lcap;
     if (m) {
         if (!inl) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
         const uint64_t pcap = m / SEG_EDGES + lcap + 1;     // pieces at most
@@ -1914,6 +1968,8 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches += 2;
         break;
       case PR_PULL_SEGMENTED:
+        k_pr_long_pieces<false><<<ctx->sm_count, PIECE_THREADS, piece_smem() + a.hub_count * 4, s>>>(a);
+        ctx->launches++;
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, LONG_INLINE, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, LONG_INLINE, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         break;
@@ -2097,6 +2153,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
                                                        : (block == PULL_WIDE ? PULL_WIDE_HUBS : PULL_NARROW_HUBS);
         a.hub_count = static_cast<uint32_t>(std::min<uint64_t>(std::min<uint64_t>(n, room), want)) & ~3u;
         const int bytes = static_cast<int>(fixed + a.hub_count * sizeof(float));
+        BW_CUDA(cudaFuncSetAttribute(k_pr_long_pieces<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(piece_smem() + a.hub_count * sizeof(float))));
         if (block == PULL_WIDE) {
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -2166,8 +2224,20 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     // launches and their order are the same
     cudaGraph_t loop_graph = nullptr;
     cudaStream_t ls = s;
+    // BW_LAUNCH_L2_WINDOW: the gathered vector persisting in L2 (div: both
+    // contribution buffers; nodiv: the rank buffers it gathers from)
+    L2Window win, win_ls;
+    const bool l2w = cfg && (cfg->flags & BW_LAUNCH_L2_WINDOW);
+    const void *l2_base = nodiv ? static_cast<const void *>(nb[0] < nb[1] ? nb[0] : nb[1])
+                                : static_cast<const void *>(ctx->pr_buf[0]);
+    const size_t l2_bytes = nodiv ? n * sizeof(float) : 2 * n * sizeof(float);
+    if (l2w) BW_TRY(l2_window_begin(ctx, s, l2_base, l2_bytes, win));
     if (loop_mode == 1) {
         BW_CUDA(cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking));
+        if (l2w) {
+            const int rc = l2_window_begin(ctx, ls, l2_base, l2_bytes, win_ls, false);
+            if (rc != BW_OK) { cudaStreamDestroy(ls); return rc; }
+        }
         const cudaError_t e = cudaStreamBeginCapture(ls, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) {
             cudaStreamDestroy(ls);
@@ -2210,6 +2280,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.piece_sum = items.piece_sum;
         a.piece_map = items.piece_map;
         a.sum_ctr = items.sum_ctr;
+        a.piece_total = items.piece_total;
         // div: rows without in-edges hold the same rank and contribution in
         // both buffers once iterations 1 and 2 have written them
         a.count_dev = items.work ? ((!nodiv && j > 2) ? items.count_nonconst : items.count_all) : nullptr;
@@ -2218,6 +2289,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     }
     if (loop_mode == 1) {
         const cudaError_t e = cudaStreamEndCapture(ls, &loop_graph);
+        l2_window_end(win_ls);
         cudaStreamDestroy(ls);
         if (loop_status == BW_OK && e != cudaSuccess) {
             set_last_error(e, "cudaStreamEndCapture");

@@ -238,6 +238,16 @@ typedef struct bw_launch_config {
  */
 #define BW_LAUNCH_RELABEL 1u
 #define BW_LAUNCH_NO_RELABEL 2u
+/*
+ * BW_LAUNCH_L2_WINDOW (no reference counterpart): for the run's kernels, an
+ * L2 access-policy window marks the randomly gathered vector persisting --
+ * PageRank's contribution buffers, BFS's depth array -- with a persisting
+ * carve-out of L2 of that size (at most the device's maximum); both are
+ * removed when the run ends.  Results are unchanged.  The window is a stream
+ * attribute, so the run's stream must be a created one (the legacy default
+ * stream returns BW_ERR_INVALID_ARGUMENT).
+ */
+#define BW_LAUNCH_L2_WINDOW 4u
 
 /* Reference Backend::computeDivision for `count` items. */
 void bw_compute_division(uint64_t count, uint32_t sm_count,

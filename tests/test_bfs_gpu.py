@@ -163,3 +163,19 @@ def test_cluster_path_overflow(ctx, leaves):
         run = bw.bfs(ctx, g, "frontier-push", 0, loop=loop, stats=True)
         assert np.array_equal(run.levels.cpu().numpy(), want), loop
         assert [s["frontier_vertices"] for s in run.level_stats] == list(cnt), loop
+
+
+@pytest.mark.parametrize("variant", ["frontier-push", "frontier-pull", "edge-list-bulk", "vertex-pull-warp"])
+@pytest.mark.parametrize("loop", ["host", "graph"])
+def test_l2_window_leaves_depths_unchanged(ctx, graphs, variant, loop):
+    """BW_LAUNCH_L2_WINDOW (the depth array persisting in L2): same depths."""
+    import torch
+    side = torch.cuda.Stream()                    # a window is an attribute of a created stream
+    for name, (h, g, r, lv, cnt) in graphs.items():
+        with torch.cuda.stream(side):
+            run = bw.bfs(ctx, g, variant, r, loop=loop, l2_window=True)
+            got = run.levels.cpu().numpy()
+        assert np.array_equal(got, lv), (variant, name, loop)
+    with pytest.raises(bw.BwError):               # the legacy default stream carries no window
+        bw.bfs(ctx, graphs["rmat10"][1], variant, graphs["rmat10"][2], l2_window=True,
+               stream=torch.cuda.default_stream())

@@ -164,15 +164,16 @@ def test_kernel_launch_count(ctx, graphs, long_graphs):
     piece count and emission, short-item count and emission), the
     hub-first order (keys, the device-side decision unless forced, slots,
     source translation -- the last two return at once when the order is not
-    taken), init, and per iteration one kernel for pull-segmented, two for
-    the exact variants (work list + long-row sums) and for the atomic ones
-    (scatter + consolidation)."""
+    taken), init, and per iteration two kernels for the staged exact
+    variants (work list + long-row sums), for the atomic ones
+    (scatter + consolidation) and for pull-segmented (long-row pieces, then
+    the short rows)."""
     _, g = graphs["rmat14"]
     assert bw.pagerank(ctx, g, "vertex-pull", 5).kernel_launches == 1 + 6 + 4 + 1 + 2 * 5
     assert bw.pagerank(ctx, g, "vertex-pull", 2).kernel_launches == 1 + 6 + 1 + 2 * 2
     assert bw.pagerank(ctx, g, "rev-edge-list", 5).kernel_launches == 1 + 1 + 2 * 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 6 + 3 + 1 + 5
-    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 6 + 1 + 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=True).kernel_launches == 1 + 6 + 3 + 1 + 2 * 5
+    assert bw.pagerank(ctx, g, "pull-segmented", 5, relabel=False).kernel_launches == 1 + 6 + 1 + 2 * 5
 
 
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented", "vertex-pull-warp"])
@@ -227,6 +228,23 @@ def test_graph_loop_matches_host_loop(ctx, graphs, long_graphs, variant):
     for name, (h, g) in [("rmat14", graphs["rmat14"]), ("star", graphs["star"])] + list(long_graphs.items()):
         want = bw.pagerank(ctx, g, variant, 12).ranks.cpu().numpy()
         got = bw.pagerank(ctx, g, variant, 12, loop="graph").ranks.cpu().numpy()
+        if variant in BITEXACT:
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (variant, name)
+        else:
+            assert _rel(got, want) <= REL_REF, (variant, name)
+
+
+@pytest.mark.parametrize("variant", ["pull-segmented", "vertex-pull-nodiv", "rev-edge-list"])
+@pytest.mark.parametrize("loop", ["host", "graph"])
+def test_l2_window_leaves_results_unchanged(ctx, graphs, long_graphs, variant, loop):
+    """BW_LAUNCH_L2_WINDOW (the gathered vector persisting in L2) changes
+    where the lines live, not what the kernels compute."""
+    import torch
+    side = torch.cuda.Stream()                    # a window is an attribute of a created stream
+    for name, (h, g) in [("rmat14", graphs["rmat14"])] + list(long_graphs.items()):
+        want = bw.pagerank(ctx, g, variant, 12, loop=loop).ranks.cpu().numpy()
+        with torch.cuda.stream(side):
+            got = bw.pagerank(ctx, g, variant, 12, loop=loop, l2_window=True).ranks.cpu().numpy()
         if variant in BITEXACT:
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (variant, name)
         else:
