@@ -66,6 +66,12 @@ def candidates(algorithm: str, name: str, sm_count: int):
     blocks = BLOCKS[kind]
     if algorithm == "pagerank" and kind in ("edge", "vertex"):
         blocks = [128, 256]                    # PageRank kernels are built for <= 256 threads
+    if algorithm == "pagerank" and kind == "fixed":
+        # work-list kernels: the block shape and the long-row threshold
+        for blk, long_row in itertools.product([0, 256], [0, 384, 512]):
+            if blk or long_row:
+                yield {k: v for k, v in (("block", blk), ("warp", long_row)) if v}
+        return
     for blk, mult in itertools.product(blocks, GRID_MULT if kind != "fixed" else [0]):
         grid = sm_count * mult if mult else 0
         if kind == "warp":

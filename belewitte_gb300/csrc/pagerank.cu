@@ -103,7 +103,6 @@ struct PrArgs {
     // Decided on the device, so the host never waits inside a run:
     const uint32_t *relabel_on;   // != 0: the hub-first order was taken (nullptr: never)
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
-    const uint32_t *piece_total;  // device: long-row pieces at the head of the list
     const float *gat_in;
     float *gat_out;
     double base_div;           // (1.0 - 0.85f) / N, computed once on the host
@@ -708,7 +707,8 @@ __global__ void __launch_bounds__(256) k_pr_heavy_finish(PrArgs a)
 // vertex-pull, vertex-pull-nodiv and pull-segmented share one kernel over a
 // work list cut once per run from the reverse CSR: an item is either at
 // most 32 consecutive rows with at most SEG_EDGES edges (rows of at most
-// SEG_LONG edges), or one long row.  Item: {row_begin, row_end | flags,
+// the long-row threshold, SEG_LONG unless the launch gives another), or a
+// piece of one long row.  Item: {row_begin, row_end | flags,
 // edge_begin, edge_end}.
 //
 // Short rows: the warp loads the item's indices with unrolled coalesced
@@ -717,18 +717,14 @@ __global__ void __launch_bounds__(256) k_pr_heavy_finish(PrArgs a)
 // row's values one after the other in row order -- the reference's
 // sequential summation (pagerank/vertex_pull.cu:23-27), so these rows are
 // bit-identical to it.
-// Long rows (more than SEG_LONG edges) are cut into SEG_EDGES-edge pieces
+// Long rows (more edges than the threshold) are cut into SEG_EDGES-edge pieces
 // that any warp takes; the work list puts every piece, longest rows first,
 // before the short-row items:
-//   staged (vertex-pull, vertex-pull-nodiv): pieces store their gathered
-//   terms in vals[] (edge order); k_pr_long_sums then evaluates every long
-//   row's sequential sum (bit-identical to the reference's loop) and
-//   consolidates it.
-//   inline (pull-segmented): the same sequential sums inside this kernel,
-//   from binade-map records of the pieces (inline_piece); no terms are
-//   staged in global memory and no second kernel runs.
+//   pieces store their gathered terms in vals[] (edge order);
+//   k_pr_long_sums then evaluates every long row's sequential sum
+//   (bit-identical to the reference's loop) and consolidates it.
 constexpr uint32_t SEG_EDGES = 512;
-constexpr uint32_t SEG_LONG = 256;
+constexpr uint32_t SEG_LONG = 256;             // default long-row threshold (at most SEG_EDGES)
 constexpr uint32_t LONG_FLAG = 0x40000000u;    // piece of a long row
 constexpr uint32_t CONST_FLAG = 0x20000000u;   // rows without in-edges
 constexpr uint32_t ROW_MASK = 0x1fffffffu;     // work-list variants take N < 2^29
@@ -740,10 +736,8 @@ constexpr uint32_t ROW_MASK = 0x1fffffffu;     // work-list variants take N < 2^
 // from shared memory instead of L2.  Every block holds its own copy, and
 // what shared memory takes is lost to L1, which bounds the misses in flight.
 constexpr int PULL_WIDE = 1024, PULL_NARROW = 256;
-// Per warp: a gather buffer of SEG_EDGES terms, padded to one extra word per
-// 32 (the layout in which a lane reads its own run of terms without bank
-// conflicts), then 33 words of row ends.
-constexpr uint32_t PULL_BUF = SEG_EDGES + SEG_EDGES / 32;
+// Per warp: a gather buffer of SEG_EDGES terms, then 33 words of row ends.
+constexpr uint32_t PULL_BUF = SEG_EDGES;
 constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (PULL_BUF + 33) * sizeof(float); }
 constexpr int pull_min_blocks(int block) { return block == PULL_WIDE ? 1 : 4; }
 // default hub-cache entries per block (measured on GB300: WIDE with 16K
@@ -758,21 +752,22 @@ constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 //    in-edges become CONST items at the end of the list (for the div
 //    variants their rank and contribution are the same from the second
 //    iteration on, so later iterations leave them out).
-//  * Long rows (more than SEG_LONG edges) are sorted by decreasing length
+//  * Long rows (more edges than the threshold) are sorted by decreasing length
 //    and cut into SEG_EDGES pieces in that order, at the front of the list.
 // Layout: [pieces | short items | CONST items]; the lengths stay on the
 // device (tot[0] = items before the CONST ones, tot[1] = all items).
-__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t *__restrict__ flag,
-                            uint32_t *__restrict__ long_flag)
+__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t seg_long,
+                            uint32_t *__restrict__ flag, uint32_t *__restrict__ long_flag)
 {
     for (uint64_t r = gtid(); r < n; r += gthreads()) {
         const uint32_t d = off[r + 1] - off[r];
         flag[r] = d ? 1u : 0u;
-        long_flag[r] = d > SEG_LONG ? 1u : 0u;
+        long_flag[r] = d > seg_long ? 1u : 0u;
     }
 }
 
-__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, const uint32_t *__restrict__ pos,
+__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, uint32_t seg_long,
+                                const uint32_t *__restrict__ pos,
                                 const uint32_t *__restrict__ long_pos, uint32_t *__restrict__ rows,
                                 uint32_t *__restrict__ long_len, uint32_t *__restrict__ long_row)
 {
@@ -781,29 +776,20 @@ __global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, co
         const uint32_t d = off[r + 1] - off[r];
         if (d) rows[pos[r]] = static_cast<uint32_t>(r);
         else rows[ne + (r - pos[r])] = static_cast<uint32_t>(r);
-        if (d > SEG_LONG) {
+        if (d > seg_long) {
             long_len[long_pos[r]] = d;
             long_row[long_pos[r]] = static_cast<uint32_t>(r);
         }
     }
 }
 
-// Pieces of a long row of n terms.  Staged (vertex-pull, vertex-pull-nodiv):
-// SEG_EDGES terms each.  Inline (pull-segmented): piece 0 is the serial
-// start, the first min(n, SERIAL_TERMS) terms, then SEG_EDGES terms each.
-__host__ __device__ __forceinline__ uint32_t row_pieces(uint32_t n, int inl)
-{
-    if (!inl) return (n + SEG_EDGES - 1) / SEG_EDGES;
-    return n <= SERIAL_TERMS ? 1u : 1u + (n - SERIAL_TERMS + SEG_EDGES - 1) / SEG_EDGES;
-}
-
 // Piece counts of the sorted long rows (0 past the last one).
 __global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
-                              uint64_t cap, int inl, uint32_t *__restrict__ pieces)
+                              uint64_t cap, uint32_t *__restrict__ pieces)
 {
     const uint64_t L = *long_total;
     for (uint64_t i = gtid(); i < cap; i += gthreads())
-        pieces[i] = i < L ? row_pieces(long_len[i], inl) : 0u;
+        pieces[i] = i < L ? (long_len[i] + SEG_EDGES - 1) / SEG_EDGES : 0u;
 }
 
 // Exact long rows above GIANT_ROW terms are summed piece-parallel (binade
@@ -817,7 +803,7 @@ constexpr uint32_t GIANT_ROW = 2048;
 // counters cleared; the number of rows above GIANT_ROW and of their pieces.
 __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ long_row,
                              const uint32_t *__restrict__ long_len, const uint32_t *__restrict__ long_total,
-                             const uint32_t *__restrict__ ppos, int inl, uint4 *__restrict__ work,
+                             const uint32_t *__restrict__ ppos, uint4 *__restrict__ work,
                              uint32_t *__restrict__ long_count, uint32_t *__restrict__ giant_total,
                              uint32_t *__restrict__ giant_pieces)
 {
@@ -834,21 +820,17 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
     for (uint64_t i = gtid(); i < L; i += gthreads()) {
         const uint32_t r = long_row[i];
         uint32_t out = ppos[i], p = off[r];
-        if (inl) {                                   // the serial start
-            const uint32_t e = min(p + SERIAL_TERMS, off[r + 1]);
-            work[out++] = make_uint4(r, (r + 1) | LONG_FLAG, p, e);
-            p = e;
-        }
+        long_count[r] = 0;
         for (; p < off[r + 1]; p += SEG_EDGES)
             work[out++] = make_uint4(r, (r + 1) | LONG_FLAG, p, min(p + SEG_EDGES, off[r + 1]));
-        long_count[r] = 0;
     }
 }
 
 // One thread per window of 32 rows of rows[0, ne): the short items it emits
 // (counts[w]); counts[W + w]: the CONST item of window w of rows[ne, N).
 __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                            const uint32_t *__restrict__ pos, uint64_t n, uint32_t *__restrict__ counts)
+                            const uint32_t *__restrict__ pos, uint64_t n, uint32_t seg_long,
+                            uint32_t *__restrict__ counts)
 {
     const uint64_t windows = (n + 31) / 32, ne = pos[n];
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
@@ -857,7 +839,7 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__
         for (uint64_t k = k0; k < k1; k++) {
             const uint32_t r = rows[k];
             const uint32_t d = off[r + 1] - off[r];
-            if (d > SEG_LONG) {                 // long rows go to pieces
+            if (d > seg_long) {                 // long rows go to pieces
                 if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
                 continue;
             }
@@ -874,7 +856,8 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__
 // contiguous: rows in between have none); CONST items
 // {ne + k0, ne + k1 | CONST, 0, 0}; both after the P pieces.
 __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                           const uint32_t *__restrict__ pos, uint64_t n, const uint32_t *__restrict__ first,
+                           const uint32_t *__restrict__ pos, uint64_t n, uint32_t seg_long,
+                           const uint32_t *__restrict__ first,
                            const uint32_t *__restrict__ piece_total, uint4 *__restrict__ work,
                            uint32_t *__restrict__ tot)
 {
@@ -892,7 +875,7 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
         for (uint64_t k = k0; k < k1; k++) {
             const uint32_t r = rows[k];
             const uint32_t d = off[r + 1] - off[r];
-            if (d > SEG_LONG) {
+            if (d > seg_long) {
                 if (acc_rows) {
                     work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
                     acc_rows = 0; acc_edges = 0;
@@ -1306,186 +1289,7 @@ __device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv
 }
 
 
-// ------------------ pull-segmented: long rows summed inline -----------------
-// Every long row's sequential sum inside the work-list kernel, bit-identical
-// to the reference's loop, with no terms staged in global memory:
-//  * Piece 0 covers the row's first min(n, SERIAL_TERMS) terms.  The warp
-//    gathers them SEG_EDGES at a time into its buffer and lane 0 adds them in
-//    row order; a row of at most SERIAL_TERMS terms ends there.
-//  * Every later piece (SEG_EDGES terms) gathers its terms into the padded
-//    layout, posts their float sum (any order) in psum[], waits for the sums
-//    of the row's earlier pieces -- neighbours in the list, processed in the
-//    same round by other warps -- and records the map of its terms under the
-//    guess those sums give, added in double (record_of_terms).  Piece 0 posts
-//    the exact running sum after the serial start.
-//  * The row's last piece to arrive combines the records in order
-//    (combine_records); a piece whose record does not hold for the true
-//    running sum is evaluated exactly by gathering its terms again.
-// A wait is bounded: one that runs out (warps not all resident, e.g. a
-// caller's grid larger than one wave) leaves its piece without a record, and
-// the combination evaluates that piece exactly, so the limit costs time,
-// never a different result.
-constexpr uint32_t PSUM_EMPTY = 0xffffffffu;       // a NaN: no sum posted yet
-constexpr uint32_t PSUM_SPIN_LIMIT = 1u << 16;
-
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
-{
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
-}
-
-// Gather src[ge[e0 + k]], k < len <= SEG_EDGES, into buf at k + k / 32 (the
-// padded layout record_of_terms reads without bank conflicts); the slots
-// past len up to SEG_EDGES get +0.  Returns this lane's partial sum.
-__device__ __forceinline__ float gather_padded(const uint32_t *__restrict__ ge, const float *__restrict__ src,
-                                               const float *hub, uint32_t hubs, uint32_t e0, uint32_t len,
-                                               float *buf, unsigned lane)
-{
-    static_assert(GATHER_UNROLL * 32 == SEG_EDGES, "one gather round per piece");
-    uint32_t idx[GATHER_UNROLL];
-#pragma unroll
-    for (int u = 0; u < GATHER_UNROLL; u++) {
-        const uint32_t k = u * 32 + lane;
-        idx[u] = k < len ? __ldcs(ge + e0 + k) : 0u;
-    }
-    float part = 0.0f;
-#pragma unroll
-    for (int u = 0; u < GATHER_UNROLL; u++) {
-        const uint32_t k = u * 32 + lane;
-        const float v = k < len ? gather1(src, hub, hubs, idx[u]) : 0.0f;
-        buf[k + (k >> 5)] = v;
-        part += v;
-    }
-    return part;
-}
-
-// What inline_piece needs of the kernel's arguments (passed apart from
-// PrArgs, so that the kernel keeps its own copy in registers).
-struct PieceIo {
-    const uint32_t *rev_v;        // reverse-CSR offsets
-    const uint32_t *ge;           // gathered-array positions of the sources
-    const float *src;             // the gathered array
-    const float *hub;             // its first `hubs` entries, in shared memory
-    uint32_t hubs;
-    uint32_t *psum;               // posted piece sums (PSUM_EMPTY: none yet)
-    uint4 *rec;                   // piece records, two uint4 each
-    uint32_t *arrivals;           // per-row arrival counters
-};
-
-// One piece of a long row; true (in every lane) when this warp summed the
-// whole row: *total is then the row's sequential sum, for the caller to
-// consolidate.
-__device__ __forceinline__ bool inline_piece(const PieceIo io, uint32_t item, uint32_t row, uint32_t e0, uint32_t e1,
-                                          float *buf, unsigned lane, float *total)
-{
-    using namespace bwseq;
-    const uint32_t *ge = io.ge;
-    const float *src = io.src, *hub = io.hub;
-    const uint32_t hubs = io.hubs;
-    const uint32_t rb = io.rev_v[row], n = io.rev_v[row + 1] - rb;
-    const uint32_t pieces = row_pieces(n, 1);
-    const uint32_t q = e0 == rb ? 0u : 1u + (e0 - rb - SERIAL_TERMS) / SEG_EDGES;
-    const uint32_t p0 = item - q;
-    uint32_t *psum = io.psum;
-    uint4 r0 = make_uint4(REC_NONE, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
-    if (q == 0) {
-        // the serial start, in row order by lane 0 (four terms per load)
-        float acc = 0.0f;
-        for (uint32_t b = e0; b < e1; b += SEG_EDGES) {
-            const uint32_t len = min(SEG_EDGES, e1 - b);
-            gather_into(ge, src, hub, hubs, b, len, buf, lane);
-            __syncwarp();
-            if (lane == 0) {
-                const float4 *b4 = reinterpret_cast<const float4 *>(buf);
-                uint32_t k = 0;
-#pragma unroll 4
-                for (; k + 4 <= len; k += 4) {
-                    const float4 v = b4[k / 4];
-                    acc = __fadd_rn(acc, v.x); acc = __fadd_rn(acc, v.y);
-                    acc = __fadd_rn(acc, v.z); acc = __fadd_rn(acc, v.w);
-                }
-                for (; k < len; k++) acc = __fadd_rn(acc, buf[k]);
-            }
-            __syncwarp();
-        }
-        const uint32_t sb = __shfl_sync(FULL_MASK, __float_as_uint(acc), 0);
-        if (pieces == 1) {
-            *total = __uint_as_float(sb);
-            return true;
-        }
-        if (lane == 0) st_release_u32(psum + item, sb);
-        r0 = make_uint4(REC_STATE, sb, 0u, 0u);
-    } else {
-        float part = gather_padded(ge, src, hub, hubs, e0, e1 - e0, buf, lane);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
-        if (lane == 0) st_release_u32(psum + item, __float_as_uint(part));
-        // the guess: the earlier pieces' sums, posted by the warps holding them
-        double pre = 0.0;
-        bool ready = true;
-        for (uint32_t i0 = 0; i0 < q && ready; i0 += 32) {
-            uint32_t bits = 0u;
-            if (i0 + lane < q) {
-                uint32_t spins = 0;
-                while ((bits = ld_acquire_u32(psum + p0 + i0 + lane)) == PSUM_EMPTY && ++spins < PSUM_SPIN_LIMIT)
-                    __nanosleep(32);
-            }
-            ready = __all_sync(FULL_MASK, bits != PSUM_EMPTY);
-            pre += static_cast<double>(__uint_as_float(bits));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
-        __syncwarp();                                 // the gathered terms are in buf
-        if (ready) {
-            uint32_t x[PIECE_L];
-#pragma unroll
-            for (uint32_t u = 0; u < PIECE_L; u++) {
-                const uint32_t k = lane * PIECE_L + u;
-                x[u] = __float_as_uint(buf[k + (k >> 5)]);
-            }
-            record_of_terms(x, __float_as_uint(__double2float_rn(pre)), lane, r0, r1);
-        }
-        __syncwarp();
-    }
-    uint32_t last = 0;
-    if (lane == 0) {
-        io.rec[2 * static_cast<uint64_t>(item)] = r0;
-        io.rec[2 * static_cast<uint64_t>(item) + 1] = r1;
-        last = atomic_add_acq_rel(&io.arrivals[row], 1u) + 1 == pieces ? 1u : 0u;
-    }
-    if (!__shfl_sync(FULL_MASK, last, 0)) return false;
-    __syncwarp();                                     // every lane's reads after lane 0's acquire
-    *total = combine_records(
-        io.rec + 2 * static_cast<uint64_t>(p0), 1u, pieces, lane,
-        [&](uint32_t qq, uint32_t sb) {
-            const uint32_t b = SERIAL_TERMS + (qq - 1) * SEG_EDGES;
-            const bool ok = warp_sequential_continue_load<PIECE_L>(
-                [&](uint32_t i) { return gather1(src, hub, hubs, __ldcg(ge + rb + i)); },
-                b, min(n, b + SEG_EDGES), sb, buf, lane);
-            return make_uint2(ok ? 1u : 0u, sb);
-        },
-        [&]() {                                       // terms outside the maps' domain
-            float t = 0.0f;
-            if (lane == 0)
-                for (uint32_t i = 0; i < n; i++) t = __fadd_rn(t, gather1(src, hub, hubs, __ldcg(ge + rb + i)));
-            return __shfl_sync(FULL_MASK, t, 0);
-        });
-    if (lane == 0) io.arrivals[row] = 0;
-    for (uint32_t i = lane; i < pieces; i += 32) psum[p0 + i] = PSUM_EMPTY;   // for the next iteration
-    return true;
-}
-
-// Long rows of the work-list kernel: staged in vals[] for k_pr_long_sums
-// (vertex-pull, vertex-pull-nodiv) or summed inline (pull-segmented).
-constexpr int LONG_STAGED = 1, LONG_INLINE = 2;
-
-template<bool NODIV, int MODE, int BLOCK>
+template<bool NODIV, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items(PrArgs a)
 {
     constexpr int PULL_WARPS = BLOCK / 32;
@@ -1504,16 +1308,13 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
         reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
     __syncthreads();
     float dsum = 0.0f;
-    // inline: the long-row pieces at the head of the list are
-    // k_pr_long_pieces' work
-    const uint64_t first = MODE == LONG_INLINE ? *a.piece_total : 0u;
     // the next item's descriptor is loaded one item ahead
-    uint4 w_next = first + warp < a.work_count ? a.work[first + warp] : make_uint4(0, 0, 0, 0);
-    for (uint64_t it = first + warp; it < a.work_count; it += warps) {
+    uint4 w_next = warp < a.work_count ? a.work[warp] : make_uint4(0, 0, 0, 0);
+    for (uint64_t it = warp; it < a.work_count; it += warps) {
         const uint4 w = w_next;
         if (it + warps < a.work_count) w_next = a.work[it + warps];
         const uint32_t r0 = w.x, r1 = w.y & ROW_MASK, e0 = w.z, e1 = w.w;
-        if (MODE == LONG_STAGED && (w.y & LONG_FLAG)) {
+        if (w.y & LONG_FLAG) {
             // exact piece: store the gathered terms in edge order (the
             // long-row sums run in k_pr_long_sums after this kernel) and
             // their float sum in any order, from which the pieces of giant
@@ -1567,44 +1368,6 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
     }
     add_diff(a.diff, dsum);
 }
-
-// pull-segmented's long rows: the pieces at the head of the work list
-// (inline_piece), one warp per piece in list order -- a row's pieces are
-// neighbours, so they run in the same round -- before k_pr_pull_items takes
-// the short rows.  Its own kernel, so that each keeps its registers: 512
-// threads, a shared-memory copy of the first hub_count entries of the
-// gathered array like the work-list kernel's.
-constexpr int PIECE_THREADS = 512;
-
-template<bool NODIV>
-__global__ void __launch_bounds__(PIECE_THREADS, 1) k_pr_long_pieces(PrArgs a)
-{
-    constexpr int WARPS = PIECE_THREADS / 32;
-    resolve_args(a);
-    extern __shared__ __align__(16) float smem_f[];
-    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
-    const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
-    float *buf = smem_f + wib * PULL_BUF;
-    float *hub = smem_f + WARPS * PULL_BUF;
-    const uint32_t hubs = a.hub_count;
-    for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
-        reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
-    __syncthreads();
-    const PieceIo io{a.rev_v, a.gat_e, src, hub, hubs, reinterpret_cast<uint32_t *>(a.piece_sum), a.piece_map,
-                     a.long_count};
-    const float base_nd = nodiv_base(a.n);
-    const uint64_t P = *a.piece_total;
-    float dsum = 0.0f;
-    for (uint64_t it = warp; it < P; it += warps) {
-        const uint4 w = a.work[it];
-        float total;
-        if (inline_piece(io, static_cast<uint32_t>(it), w.x, w.z, w.w, buf, lane, &total) && lane == 0)
-            dsum += finish_vertex<NODIV>(a, w.x, total, base_nd);
-    }
-    add_diff(a.diff, dsum);
-}
-constexpr size_t piece_smem() { return (PIECE_THREADS / 32) * PULL_BUF * sizeof(float); }
 
 // Long-row sums of the exact variants (vertex-pull, vertex-pull-nodiv),
 // after the iteration's work-list kernel has stored every long row's terms
@@ -1737,7 +1500,6 @@ struct PrRun {
     float *piece_sum = nullptr;        // exact pieces: their float sums
     uint4 *piece_map = nullptr;        // giant-row pieces: records (two uint4 each)
     uint32_t *sum_ctr = nullptr;       // k_pr_long_sums' job and finish counters
-    const uint32_t *piece_total = nullptr;     // device: pieces at the head of the list
     const uint32_t *count_all = nullptr;       // device: items in the list
     const uint32_t *count_nonconst = nullptr;  // device: items before the CONST ones
 };
@@ -1775,6 +1537,8 @@ int validate_cfg(const bw_context *ctx, int variant, const bw_launch_config *cfg
         if (cfg->block_size && cfg->block_size != PULL_WIDE && cfg->block_size != PULL_NARROW)
             return BW_ERR_INVALID_ARGUMENT;
         if (cfg->chunk_size % 4) return BW_ERR_INVALID_ARGUMENT;
+        // warp_size: the long-row threshold, a row of at most it fits an item
+        if (cfg->warp_size > SEG_EDGES) return BW_ERR_INVALID_ARGUMENT;
         return BW_OK;
     }
     if (cfg->block_size && (cfg->block_size % 32 || cfg->block_size > 256)) {
@@ -1826,12 +1590,12 @@ int launch_degrees(bw_context *ctx, const bw_graph_view *g, int variant, uint32_
     return BW_OK;
 }
 
-int build_segments(bw_context *ctx, const bw_graph_view *g, int inl, PrRun &run, cudaStream_t s)
+int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, PrRun &run, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count, m = g->edge_count;
     if (n > ROW_MASK) return BW_ERR_TOO_LARGE;
     const uint64_t windows = (n + 31) / 32;
-    const uint64_t lcap = m / (SEG_LONG + 1) + 1;          // long rows at most
+    const uint64_t lcap = m / (seg_long + 1) + 1;          // long rows at most
     // Pieces <= M / SEG_EDGES + lcap; short items <= N + W; CONST <= W.
     const uint64_t cap = 2 * windows + n + m / SEG_EDGES + lcap + 16;
     size_t t_scan_n = 0, t_scan_l = 0, t_scan_w = 0, t_sort = 0;
@@ -1875,41 +1639,38 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, int inl, PrRun &run,
     run.giant_pieces = tot + 5;
     const unsigned grid = ctx->sm_count * 4;
     // 1. row classes and the partition
-    k_row_flags<<<grid, 256, 0, s>>>(g->rev_vertices, n, flag, lflag);
+    k_row_flags<<<grid, 256, 0, s>>>(g->rev_vertices, n, seg_long, flag, lflag);
     BW_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
     BW_CUDA(cudaMemsetAsync(lflag + n, 0, sizeof(uint32_t), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, flag, pos, static_cast<int64_t>(n + 1), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, lflag, lpos, static_cast<int64_t>(n + 1), s));
     BW_CUDA(cudaMemsetAsync(S + o_lkey0, 0, lcap * sizeof(uint32_t), s));   // past the last long row: length 0
-    k_row_partition<<<grid, 256, 0, s>>>(g->rev_vertices, n, pos, lpos, run.rows, S + o_lkey0, S + o_lid0);
+    k_row_partition<<<grid, 256, 0, s>>>(g->rev_vertices, n, seg_long, pos, lpos, run.rows, S + o_lkey0, S + o_lid0);
     // 2. long rows by decreasing length (stable), their pieces in that order
     lkeys = cub::DoubleBuffer<uint32_t>(S + o_lkey0, S + o_lkey1);
     lids = cub::DoubleBuffer<uint32_t>(S + o_lid0, S + o_lid1);
     BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
     run.long_rows = lids.Current();
-    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, inl, pcnt);
+    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, pcnt);
     BW_CUDA(cudaMemsetAsync(pcnt + lcap, 0, sizeof(uint32_t), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
-                                      inl, run.work, run.long_count, run.giant_total, run.giant_pieces);
+                                      run.work, run.long_count, run.giant_total, run.giant_pieces);
     BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
-    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, wcnt);
+    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, wcnt);
     BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_w, wcnt, first, static_cast<int64_t>(2 * windows + 1), s));
-    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, first, ppos + lcap, run.work, tot);
+    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, first, ppos + lcap, run.work, tot);
     ctx->launches += 6;                  // flags, partition, piece count/emit, count, emit (scans, sort: library)
     BW_CUDA(cudaGetLastError());
     run.count_nonconst = tot;
     run.count_all = tot + 1;
-    run.piece_total = ppos + lcap;
     if (m) {
-        if (!inl) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
         const uint64_t pcap = m / SEG_EDGES + lcap + 1;     // pieces at most
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_map), 2 * pcap * sizeof(uint4), s));
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_sum), pcap * sizeof(float), s));
-        // inline: every posted piece sum starts empty (PSUM_EMPTY)
-        if (inl) BW_CUDA(cudaMemsetAsync(run.piece_sum, 0xff, pcap * sizeof(float), s));
     }
     return BW_OK;
 }
@@ -1944,14 +1705,14 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches++;
         break;
       case PR_VERTEX_PULL:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, LONG_STAGED, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, LONG_STAGED, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_NODIV:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<true, LONG_STAGED, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<true, LONG_STAGED, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        if (geo.block == PULL_WIDE) k_pr_pull_items<true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         k_pr_long_sums<true><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
         break;
@@ -1968,10 +1729,11 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches += 2;
         break;
       case PR_PULL_SEGMENTED:
-        k_pr_long_pieces<false><<<ctx->sm_count, PIECE_THREADS, piece_smem() + a.hub_count * 4, s>>>(a);
+        // the vertex-pull kernel pair under the variant's own tuned shape
+        if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
         ctx->launches++;
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, LONG_INLINE, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, LONG_INLINE, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         break;
       default: return BW_ERR_UNKNOWN_VARIANT;
     }
@@ -2086,7 +1848,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         return BW_ERR_INVALID_ARGUMENT;
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
-    bool need_inline = false, need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
+    bool need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
          all_items = true;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
@@ -2095,8 +1857,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         if (is_nodiv(v) != nodiv) return BW_ERR_INVALID_ARGUMENT;
         BW_TRY(validate_cfg(ctx, v, cfg));
         reps |= kPrReps[v];
-        if (v == PR_PULL_SEGMENTED) need_inline = true;
-        if (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV) need_exact = true;
+        if (v == PR_PULL_SEGMENTED || v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV) need_exact = true;
         if (v == PR_VERTEX_PUSH || v == PR_VERTEX_PUSH_WARP || v == PR_VERTEX_PULL_WARP ||
             v == PR_VERTEX_PULL_WARP_NODIV)
             need_heavy = true;
@@ -2115,9 +1876,11 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     ctx->launches = 0;
     if (time_iterations) BW_TRY(ensure_level_events(ctx, iterations + 1));
 
-    PrRun inline_run, exact_run;
-    if (need_inline) BW_TRY(build_segments(ctx, g, 1, inline_run, s));
-    if (need_exact) BW_TRY(build_segments(ctx, g, 0, exact_run, s));
+    PrRun exact_run;
+    // the long-row threshold: warp_size of the work-list variants' launch
+    // configuration (0: SEG_LONG), rows up to it summed in the work-list kernel
+    const uint32_t seg_long = (cfg && cfg->warp_size) ? cfg->warp_size : SEG_LONG;
+    if (need_exact) BW_TRY(build_segments(ctx, g, seg_long, exact_run, s));
     // heavy-unit tiles of the push and warp-pull variants
     uint4 *heavy_q = nullptr;
     uint32_t *heavy_small = nullptr;                 // 8 counters, then the chunk list
@@ -2140,7 +1903,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.deg = ctx->pr_deg;
     a.acc = ctx->pr_acc;
     a.gat_e = g->rev_edges;
-    if (need_inline || need_exact) {
+    if (need_exact) {
         // hub cache entries per block: chunk_size when given, else the
         // default for the shape; never more than the block's share of
         // shared memory allows
@@ -2153,16 +1916,12 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
                                                        : (block == PULL_WIDE ? PULL_WIDE_HUBS : PULL_NARROW_HUBS);
         a.hub_count = static_cast<uint32_t>(std::min<uint64_t>(std::min<uint64_t>(n, room), want)) & ~3u;
         const int bytes = static_cast<int>(fixed + a.hub_count * sizeof(float));
-        BW_CUDA(cudaFuncSetAttribute(k_pr_long_pieces<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(piece_smem() + a.hub_count * sizeof(float))));
         if (block == PULL_WIDE) {
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, LONG_STAGED, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_INLINE, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         } else {
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_STAGED, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, LONG_STAGED, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, LONG_INLINE, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         }
     }
     a.warp_size = (cfg && cfg->warp_size) ? cfg->warp_size : 32;
@@ -2190,7 +1949,6 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, s);
         if (rc != BW_OK) {
             free_relabel(rl, s);
-            free_run(inline_run, s);
             free_run(exact_run, s);
             return rc;
         }
@@ -2268,7 +2026,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
                 a.contrib_out = contrib[j & 1];
             }
         }
-        const PrRun &items = v == PR_PULL_SEGMENTED ? inline_run : exact_run;
+        const PrRun &items = exact_run;
         a.work = items.work;
         a.long_count = items.long_count;
         a.vals = items.vals;
@@ -2280,7 +2038,6 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.piece_sum = items.piece_sum;
         a.piece_map = items.piece_map;
         a.sum_ctr = items.sum_ctr;
-        a.piece_total = items.piece_total;
         // div: rows without in-edges hold the same rank and contribution in
         // both buffers once iterations 1 and 2 have written them
         a.count_dev = items.work ? ((!nodiv && j > 2) ? items.count_nonconst : items.count_all) : nullptr;
@@ -2317,7 +2074,6 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         BW_CUDA(cudaMemcpyAsync(&diffs_dev_last, ctx->pr_diffs + iterations - 1, sizeof(float),
                                 cudaMemcpyDeviceToHost, s));
     BW_CUDA(cudaStreamSynchronize(s));
-    free_run(inline_run, s);
     free_run(exact_run, s);
     free_relabel(rl, s);
     if (heavy_q) cudaFreeAsync(heavy_q, s);

@@ -228,7 +228,10 @@ typedef struct bw_launch_config {
  * Work-list PageRank variants (vertex-pull, vertex-pull-nodiv,
  * pull-segmented): block_size 1024 (default) or 256 picks the block shape,
  * chunk_size the number of gathered-array entries each block caches in
- * shared memory (0 = default, multiple of 4).  Relabelling stores the
+ * shared memory (0 = default, multiple of 4), warp_size the long-row
+ * threshold (0 = 256, at most 512): rows with more in-edges are cut into
+ * pieces whose sequential sums a second kernel evaluates, shorter ones are
+ * summed where they are gathered.  Relabelling stores the
  * gathered array in decreasing out-degree order so that the cached entries
  * are the hubs; it costs one pass over the edges per run and leaves every
  * result unchanged.  By default it runs when the cached entries would cover

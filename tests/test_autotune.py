@@ -15,8 +15,10 @@ def test_candidates_start_with_the_library_default():
         assert cands[0] == {}
         assert len(cands) == len({json.dumps(c, sort_keys=True) for c in cands})      # no repeats
         for c in cands[1:]:
-            if "warp" in c:
+            if "chunk" in c:                                      # warp variants: the virtual warp
                 assert c["block"] % c["warp"] == 0 and c["chunk"] % c["warp"] == 0
+            elif "warp" in c:                                     # work-list kernels: the long-row threshold
+                assert algo == "pagerank" and c["warp"] <= 512
 
 
 def test_tune_keeps_the_fastest_and_writes_both_caches(tmp_path, monkeypatch):

@@ -114,15 +114,17 @@ def test_long_rows(ctx, long_graphs, variant, iterations):
 
 
 @pytest.mark.parametrize("variant", ["vertex-pull", "vertex-pull-nodiv", "pull-segmented"])
-@pytest.mark.parametrize("block,hubs", [(256, 0), (256, 4), (256, 2048), (1024, 0), (1024, 16384), (1024, 1 << 20)])
+@pytest.mark.parametrize("block,hubs,long_row", [(256, 0, 0), (256, 4, 512), (256, 2048, 64), (1024, 0, 300),
+                                                  (1024, 16384, 0), (1024, 16384, 512), (1024, 1 << 20, 1)])
 @pytest.mark.parametrize("relabel", [False, True])
-def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs, relabel):
+def test_pull_shapes(ctx, graphs, long_graphs, variant, block, hubs, long_row, relabel):
     """Both block shapes of the work-list kernels, with and without the
     shared-memory hub cache (sizes beyond the graph or the shared memory
-    are clamped) and the hub-first source order: results do not depend on
-    any of them."""
+    are clamped), long-row thresholds from 1 to 512 and the hub-first
+    source order: results do not depend on any of them."""
     for name, (h, g) in list(long_graphs.items()) + [("rmat14", graphs["rmat14"]), ("chain", graphs["chain"])]:
-        got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs, relabel=relabel).ranks.cpu().numpy()
+        got = bw.pagerank(ctx, g, variant, 30, block=block, chunk=hubs, warp=long_row,
+                          relabel=relabel).ranks.cpu().numpy()
         div, nodiv, d64, n64 = _oracles(h, 30)
         ref = nodiv if "nodiv" in variant else div
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (variant, name, block, hubs)
