@@ -48,10 +48,11 @@ from ._abi import check
 CANDIDATES = ["edge-list-bulk", "rev-edge-list-bulk", "struct-edge-list-bulk", "rev-struct-edge-list-bulk",
               "vertex-pull-bulk", "vertex-pull-warp-bulk", "frontier-push", "frontier-pull"]
 PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "bfs_predictor.npz"
-# PageRank: every variant of the div semantics class (a schedule cannot mix
-# it with the nodiv variants, whose ranks differ by construction)
+# PageRank: every reference variant of the div semantics class (a schedule
+# cannot mix it with the nodiv variants, whose ranks differ by construction;
+# pull-segmented runs vertex-pull's kernels)
 PR_CANDIDATES = ["edge-list", "rev-edge-list", "struct-edge-list", "rev-struct-edge-list", "vertex-push",
-                 "vertex-pull", "vertex-push-warp", "vertex-pull-warp", "pull-segmented"]
+                 "vertex-pull", "vertex-push-warp", "vertex-pull-warp"]
 PR_PREDICTOR_PATH = Path(__file__).resolve().parent / "data" / "pagerank_predictor.npz"
 PR_PROFILE_ITERATIONS = 8      # timed per candidate: the first iteration, then the steady state
 PR_RUN_ITERATIONS = 30         # the run a profile stands for
@@ -270,14 +271,15 @@ def profile_pagerank(ctx, g, candidates=PR_CANDIDATES, iterations: int = PR_PROF
     row 0 the first iteration, row 1 the other run_iterations - 1 at the
     steady-state rate (median of the last half of `iterations` timed
     iterations: some variants settle after the first few, e.g.
-    pull-segmented takes its hub-first order).  Every candidate runs alone
+    vertex-pull takes its hub-first order).  Every candidate runs alone
     after a warm-up run, timed per iteration with CUDA events
     (pagerank_schedule)."""
     from . import pagerank, pagerank_schedule
     times = np.zeros((2, len(candidates)), np.float32)
     for k, v in enumerate(candidates):
-        pagerank(ctx, g, v, 1)
-        run = pagerank_schedule(ctx, g, [v], iterations, time_iterations=True)
+        # the library's default launch: what the learned run executes
+        pagerank(ctx, g, v, 1, tuned=False)
+        run = pagerank_schedule(ctx, g, [v], iterations, time_iterations=True, tuned=False)
         t = np.asarray(run.iteration_ms[:iterations], np.float64)
         times[0, k] = t[0]
         times[1, k] = np.median(t[iterations // 2:]) * (run_iterations - 1)
