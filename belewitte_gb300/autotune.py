@@ -66,6 +66,8 @@ def candidates(algorithm: str, name: str, sm_count: int):
     blocks = BLOCKS[kind]
     if algorithm == "pagerank" and kind in ("edge", "vertex"):
         blocks = [128, 256]                    # PageRank kernels are built for <= 256 threads
+    if algorithm == "pagerank" and name in ("edge-list", "struct-edge-list"):
+        return                                 # their hot-destination kernel has one geometry
     if algorithm == "pagerank" and kind == "fixed":
         # work-list kernels: the block shape and the long-row threshold
         for blk, long_row in itertools.product([0, 256], [0, 384, 512]):

@@ -102,9 +102,12 @@ int ensure_pr_scratch(bw_context *ctx, uint64_t n, uint32_t iterations)
     if (n > ctx->pr_n_cap) {
         BW_TRY(grow(&ctx->pr_acc, n));
         // both contribution buffers in one allocation, so one L2
-        // access-policy window covers the vector every iteration gathers
-        BW_TRY(grow(&ctx->pr_buf[0], 2 * n));
-        ctx->pr_buf[1] = ctx->pr_buf[0] + n;
+        // access-policy window covers the vector every iteration gathers;
+        // the second starts on a 256-byte boundary (the kernels read both
+        // with 16-byte vector loads)
+        const uint64_t stride = (n + 63) & ~uint64_t(63);
+        BW_TRY(grow(&ctx->pr_buf[0], 2 * stride));
+        ctx->pr_buf[1] = ctx->pr_buf[0] + stride;
         BW_TRY(grow(&ctx->pr_deg, n));
         ctx->pr_n_cap = n;
     }

@@ -105,6 +105,13 @@ struct PrArgs {
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
     const float *gat_in;
     float *gat_out;
+    // Forward edge lists: the destination stream with the hot destinations
+    // (the most edges in) replaced by HOT_BIT | their slot, and the vertex
+    // of each slot (k_pr_edge_hot); nullptr: not built.
+    const uint32_t *hot_dst;      // edge-list: translated outEdges
+    const uint2 *hot_pairs;       // struct-edge-list: translated {in, out}
+    const uint32_t *hot_vertex;
+    const uint32_t *hot_count;    // device: slots in use
     double base_div;           // (1.0 - 0.85f) / N, computed once on the host
 };
 
@@ -344,6 +351,111 @@ __global__ void __launch_bounds__(256) k_pr_edge(PrArgs a)
             if (e < m) atomicAdd(&a.acc[dst], val);
         }
     }
+}
+
+// -------------------- forward edge lists: hot destinations ------------------
+// edgeListPageRank and structEdgeListPageRank (pagerank/edgelist.cu:3-23,
+// struct_edgelist.cu) add every edge's contribution to its destination with
+// one float atomic.  On a skewed graph a few thousand destinations take a
+// third of the edges, and atomics on one address serialise in L2.  Once per
+// run the destinations with the most in-edges (whole log2 classes of the
+// in-degree, at most HOT_SLOTS of them) get a slot, and the destination
+// stream is rewritten with HOT_BIT | slot in their place.  Each block then
+// adds those edges into its own shared-memory copy of the hot accumulators
+// and flushes each nonzero slot to acc[] with one atomic when its edges are
+// done; every other edge is added as before.  Float-atomic order is the
+// variants' own (the reference's is unspecified), so results stay within
+// the order-changing variants' tolerance.
+constexpr uint32_t HOT_SLOTS = 16384;          // 64 KB of accumulators per block
+constexpr uint32_t HOT_BIT = 0x80000000u;
+constexpr int HOT_THREADS = 1024;
+
+// 33 counters: vertices by floor(log2(in-degree)) (class 32: in-degree 0)
+__global__ void k_hot_classes(const uint32_t *__restrict__ indeg, uint64_t n, uint32_t *__restrict__ bins)
+{
+    __shared__ uint32_t b[33];
+    if (threadIdx.x < 33) b[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t v = gtid(); v < n; v += gthreads()) {
+        const uint32_t d = indeg[v];
+        atomicAdd(&b[d ? 31 - __clz(d) : 32], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 33 && b[threadIdx.x]) atomicAdd(&bins[threadIdx.x], b[threadIdx.x]);
+}
+
+// bins[33] = the lowest class taken: the top classes while they fit the
+// slots (classes of in-degree below 2 are never taken)
+__global__ void k_hot_pick(uint32_t *bins)
+{
+    if (blockIdx.x || threadIdx.x) return;
+    uint32_t total = 0, lowest = 32;
+    for (int c = 31; c >= 1; c--) {
+        if (total + bins[c] > HOT_SLOTS) break;
+        total += bins[c];
+        lowest = static_cast<uint32_t>(c);
+    }
+    bins[33] = lowest;
+    bins[34] = 0;                                  // slot counter
+}
+
+__global__ void k_hot_assign(const uint32_t *__restrict__ indeg, uint64_t n, uint32_t *__restrict__ bins,
+                             uint32_t *__restrict__ slot_of, uint32_t *__restrict__ hot_vertex)
+{
+    const uint32_t lowest = bins[33];
+    for (uint64_t v = gtid(); v < n; v += gthreads()) {
+        const uint32_t d = indeg[v];
+        uint32_t sl = 0xffffffffu;
+        if (lowest < 32 && d && static_cast<uint32_t>(31 - __clz(d)) >= lowest) {
+            sl = atomicAdd(&bins[34], 1u);
+            hot_vertex[sl] = static_cast<uint32_t>(v);
+        }
+        slot_of[v] = sl;
+    }
+}
+
+// PAIRS: {in, out} pairs (struct-edge-list), else the outEdges stream
+template<bool PAIRS>
+__global__ void __launch_bounds__(256) k_hot_translate(const uint32_t *__restrict__ dst, const uint2 *__restrict__ pairs,
+                                                       uint64_t m, const uint32_t *__restrict__ slot_of,
+                                                       uint32_t *__restrict__ out, uint2 *__restrict__ out_pairs)
+{
+    for (uint64_t e = gtid(); e < m; e += gthreads()) {
+        if constexpr (PAIRS) {
+            uint2 p = __ldcs(pairs + e);
+            const uint32_t sl = slot_of[p.y];
+            if (sl != 0xffffffffu) p.y = HOT_BIT | sl;
+            __stcs(out_pairs + e, p);
+        } else {
+            const uint32_t d = __ldcs(dst + e), sl = slot_of[d];
+            __stcs(out + e, sl != 0xffffffffu ? (HOT_BIT | sl) : d);
+        }
+    }
+}
+
+template<int LAYOUT>  // 0 fwd SoA, 2 fwd AoS
+__global__ void __launch_bounds__(HOT_THREADS) k_pr_edge_hot(PrArgs a)
+{
+    extern __shared__ float hot[];                 // HOT_SLOTS floats
+    const uint32_t slots = *a.hot_count;
+    for (uint32_t i = threadIdx.x; i < slots; i += blockDim.x) hot[i] = 0.0f;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
+    const uint64_t m = a.m;
+    for (uint64_t base = warp * 32; base < m; base += warps * 32) {
+        const uint64_t e = base + lane;
+        if (e >= m) continue;
+        uint32_t src, dst;
+        if constexpr (LAYOUT == 0) { src = __ldcs(a.fwd_in + e); dst = __ldcs(a.hot_dst + e); }
+        else { const uint2 p = __ldcs(a.hot_pairs + e); src = p.x; dst = p.y; }
+        const float val = __ldg(a.contrib_in + src);
+        if (dst & HOT_BIT) atomicAdd(&hot[dst & ~HOT_BIT], val);
+        else atomicAdd(&a.acc[dst], val);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < slots; i += blockDim.x)
+        if (hot[i] != 0.0f) atomicAdd(&a.acc[a.hot_vertex[i]], hot[i]);
 }
 
 // ----------------------------- vertex-push --------------------------------
@@ -1690,9 +1802,15 @@ void free_run(PrRun &run, cudaStream_t s)
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
 {
     switch (variant) {
-      case PR_EDGE_LIST: k_pr_edge<0><<<geo.grid, geo.block, 0, s>>>(a); break;
+      case PR_EDGE_LIST:
+        if (a.hot_dst) k_pr_edge_hot<0><<<ctx->sm_count * 2, HOT_THREADS, HOT_SLOTS * sizeof(float), s>>>(a);
+        else k_pr_edge<0><<<geo.grid, geo.block, 0, s>>>(a);
+        break;
       case PR_REV_EDGE_LIST: k_pr_edge<1><<<geo.grid, geo.block, 0, s>>>(a); break;
-      case PR_STRUCT_EDGE_LIST: k_pr_edge<2><<<geo.grid, geo.block, 0, s>>>(a); break;
+      case PR_STRUCT_EDGE_LIST:
+        if (a.hot_pairs) k_pr_edge_hot<2><<<ctx->sm_count * 2, HOT_THREADS, HOT_SLOTS * sizeof(float), s>>>(a);
+        else k_pr_edge<2><<<geo.grid, geo.block, 0, s>>>(a);
+        break;
       case PR_REV_STRUCT_EDGE_LIST: k_pr_edge<3><<<geo.grid, geo.block, 0, s>>>(a); break;
       case PR_VERTEX_PUSH:
         k_pr_vertex_push<<<geo.grid, geo.block, 0, s>>>(a);
@@ -1849,7 +1967,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     const bool nodiv = is_nodiv(schedule[0]);
     int reps = 0;
     bool need_exact = false, need_heavy = false, any_rowlen = false, any_deg = false,
-         all_items = true;
+         all_items = true, hot_el = false, hot_st = false;
     for (uint32_t i = 0; i < schedule_len; i++) {
         const int v = schedule[i];
         all_items = all_items && (v == PR_VERTEX_PULL || v == PR_VERTEX_PULL_NODIV || v == PR_PULL_SEGMENTED);
@@ -1862,6 +1980,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
             v == PR_VERTEX_PULL_WARP_NODIV)
             need_heavy = true;
         if (uses_rowlen(v)) any_rowlen = true; else any_deg = true;
+        if (v == PR_EDGE_LIST) hot_el = true;
+        if (v == PR_STRUCT_EDGE_LIST) hot_st = true;
     }
     if (g->edge_count == 0) {
         if (!g->fwd_vertices && !g->rev_vertices) return BW_ERR_MISSING_REPRESENTATION;
@@ -1957,6 +2077,51 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         a.gat_e = rl.gat_e;
         a.relabel_on = rl.on;
     }
+    // forward edge lists: the hot destinations' slots and the rewritten
+    // destination stream, once per run (inside the timed region)
+    uint32_t *hot_buf = nullptr, *hot_dst_buf = nullptr;
+    uint2 *hot_pairs_buf = nullptr;
+    if ((hot_el || hot_st) && n < HOT_BIT) {
+        BW_CUDA(cudaFuncSetAttribute(k_pr_edge_hot<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(HOT_SLOTS * sizeof(float))));
+        BW_CUDA(cudaFuncSetAttribute(k_pr_edge_hot<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(HOT_SLOTS * sizeof(float))));
+        uint32_t *indeg = nullptr;
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&hot_buf),
+                                 (2 * n + HOT_SLOTS + 64) * sizeof(uint32_t), s));
+        indeg = hot_buf;
+        uint32_t *slot_of = hot_buf + n, *hot_vertex = hot_buf + 2 * n, *bins = hot_buf + 2 * n + HOT_SLOTS;
+        const unsigned grid = ctx->sm_count * 4;
+        if (g->rev_vertices) {
+            k_row_lengths<<<grid, 256, 0, s>>>(g->rev_vertices, n, indeg);      // in-degrees
+        } else {
+            BW_CUDA(cudaMemsetAsync(indeg, 0, n * sizeof(uint32_t), s));
+            if (hot_el) k_count_ids<<<grid * 2, 256, 0, s>>>(g->fwd_edges, g->edge_count, 1, indeg);
+            else k_count_ids<<<grid * 2, 256, 0, s>>>(g->fwd_struct_edges + 1, g->edge_count, 2, indeg);
+        }
+        BW_CUDA(cudaMemsetAsync(bins, 0, 64 * sizeof(uint32_t), s));
+        k_hot_classes<<<grid, 256, 0, s>>>(indeg, n, bins);
+        k_hot_pick<<<1, 32, 0, s>>>(bins);
+        k_hot_assign<<<grid, 256, 0, s>>>(indeg, n, bins, slot_of, hot_vertex);
+        ctx->launches += 4;
+        if (hot_el) {
+            BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&hot_dst_buf), g->edge_count * sizeof(uint32_t), s));
+            k_hot_translate<false><<<grid * 2, 256, 0, s>>>(g->fwd_edges, nullptr, g->edge_count, slot_of,
+                                                             hot_dst_buf, nullptr);
+            ctx->launches++;
+            a.hot_dst = hot_dst_buf;
+        }
+        if (hot_st) {
+            BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&hot_pairs_buf), g->edge_count * sizeof(uint2), s));
+            k_hot_translate<true><<<grid * 2, 256, 0, s>>>(nullptr, a.fwd_s, g->edge_count, slot_of, nullptr,
+                                                            hot_pairs_buf);
+            ctx->launches++;
+            a.hot_pairs = hot_pairs_buf;
+        }
+        a.hot_vertex = hot_vertex;
+        a.hot_count = bins + 34;
+        BW_CUDA(cudaGetLastError());
+    }
     // nodiv + relabelled sources: the gathered copy of the ranks, in slot order
     float *gat[2] = {ctx->pr_buf[1], ctx->pr_acc};
     const bool nodiv_gat = nodiv && relabel;
@@ -1988,7 +2153,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     const bool l2w = cfg && (cfg->flags & BW_LAUNCH_L2_WINDOW);
     const void *l2_base = nodiv ? static_cast<const void *>(nb[0] < nb[1] ? nb[0] : nb[1])
                                 : static_cast<const void *>(ctx->pr_buf[0]);
-    const size_t l2_bytes = nodiv ? n * sizeof(float) : 2 * n * sizeof(float);
+    const size_t l2_bytes = nodiv ? n * sizeof(float)
+                                  : static_cast<size_t>(ctx->pr_buf[1] - ctx->pr_buf[0] + n) * sizeof(float);
     if (l2w) BW_TRY(l2_window_begin(ctx, s, l2_base, l2_bytes, win));
     if (loop_mode == 1) {
         BW_CUDA(cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking));
@@ -2078,6 +2244,9 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     free_relabel(rl, s);
     if (heavy_q) cudaFreeAsync(heavy_q, s);
     if (heavy_small) cudaFreeAsync(heavy_small, s);
+    if (hot_buf) cudaFreeAsync(hot_buf, s);
+    if (hot_dst_buf) cudaFreeAsync(hot_dst_buf, s);
+    if (hot_pairs_buf) cudaFreeAsync(hot_pairs_buf, s);
     if (time_iterations && iteration_ms) {
         for (uint32_t j = 0; j < iterations; j++)
             BW_CUDA(cudaEventElapsedTime(&iteration_ms[j], ctx->level_events[j], ctx->level_events[j + 1]));

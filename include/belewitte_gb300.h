@@ -225,6 +225,11 @@ typedef struct bw_launch_config {
 } bw_launch_config;
 
 /*
+ * The forward edge-list PageRank variants (edge-list, struct-edge-list) run
+ * with one geometry, two 1024-thread blocks per SM: each block keeps the
+ * hottest destinations' accumulators in shared memory (block_size and
+ * grid_size do not apply to them).
+ *
  * Work-list PageRank variants (vertex-pull, vertex-pull-nodiv,
  * pull-segmented): block_size 1024 (default) or 256 picks the block shape,
  * chunk_size the number of gathered-array entries each block caches in

@@ -251,3 +251,28 @@ def test_l2_window_leaves_results_unchanged(ctx, graphs, long_graphs, variant, l
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (variant, name)
         else:
             assert _rel(got, want) <= REL_REF, (variant, name)
+
+
+@pytest.mark.parametrize("n_graph", ["grid_odd", "ba_odd"])
+def test_fresh_context_odd_vertex_count(n_graph):
+    """A context whose first graph has a vertex count that is not a multiple
+    of 4: both contribution buffers it allocates are gathered with 16-byte
+    vector loads (the hub cache), so both must start aligned.  Every variant,
+    several iterations, against the oracle."""
+    h = bw.HostGraph.grid(37, 41) if n_graph == "grid_odd" else bw.HostGraph.barabasi_albert(70001, 3, seed=5)
+    assert h.vertex_count % 4 != 0
+    c = bw.Context(0)
+    try:
+        g = bw.DeviceGraph(h)
+        div, _ = oracle.pagerank(oracle.PR_DIV, h.vertex_count, h.rev_vertices, h.rev_edges, 7)
+        nodiv, _ = oracle.pagerank(oracle.PR_NODIV, h.vertex_count, h.rev_vertices, h.rev_edges, 7)
+        for name in bw.pagerank_variant_names():
+            for loop in ("host", "graph"):
+                got = bw.pagerank(c, g, name, 7, loop=loop).ranks.cpu().numpy()
+                ref = nodiv if "nodiv" in name else div
+                if name in BITEXACT:
+                    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (name, loop)
+                else:
+                    assert _rel(got, ref) <= REL_REF, (name, loop)
+    finally:
+        c.close()
