@@ -1018,7 +1018,7 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
 // kernel).
 __device__ __forceinline__ float lane_sequential_sum(const float *p, uint32_t len)
 {
-    constexpr uint32_t Q = 8;                     // quads per stage
+    constexpr uint32_t Q = 12;                    // quads per stage (8: 1.5% slower on R-MAT-22)
     float acc = 0.0f;
     uint32_t i = 0;
     while (i < len && (reinterpret_cast<uintptr_t>(p + i) & 15)) acc = __fadd_rn(acc, __ldcg(p + i++));
@@ -1507,19 +1507,24 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
 // giant row's combining piece resets the row's arrival counter.
 constexpr int LONG_SUM_THREADS = 256;
 constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
-template<bool NODIV>
+// JOBS: 0 both job kinds (one launch), 1 the batches only, 2 the giant
+// rows' pieces only (two launches, each with its own counters: ctr[0..1]
+// and ctr[2..3]).
+template<bool NODIV, int JOBS>
 __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr_long_sums(PrArgs a, uint32_t *ctr)
 {
     __shared__ __align__(16) float stage[LONG_SUM_THREADS / 32][33 * PIECE_L];
     resolve_args(a);
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t L = *a.long_total, G = *a.giant_total, PG = *a.giant_pieces;
-    const uint32_t MB = (L - G + 31) / 32, jobs = MB + PG;
+    const uint32_t MB = (L - G + 31) / 32;
+    const uint32_t first = JOBS == 2 ? MB : 0u, jobs = JOBS == 1 ? MB : MB + PG;
+    if (JOBS == 2) ctr += 2;
     const float base_nd = nodiv_base(a.n);
     float dsum = 0.0f;
     for (;;) {
         uint32_t job = 0;
-        if (lane == 0) job = atomicAdd(&ctr[0], 1u);
+        if (lane == 0) job = first + atomicAdd(&ctr[0], 1u);
         job = __shfl_sync(FULL_MASK, job, 0);
         if (job >= jobs) break;
         if (job < MB) {
@@ -1735,7 +1740,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     const uint64_t o_ppos = at; at += al(lcap + 1);
     const uint64_t o_wcnt = at; at += al(2 * windows + 1);
     const uint64_t o_first = at; at += al(2 * windows + 1);
-    const uint64_t o_tot = at; at += al(6);
+    const uint64_t o_tot = at; at += al(12);   // lengths, giant rows, long-sum counters (tot + 8)
     const uint64_t o_temp = at;
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.scratch), o_temp * sizeof(uint32_t) + temp, s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
@@ -1747,7 +1752,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     uint32_t *pcnt = S + o_pcnt, *ppos = S + o_ppos, *wcnt = S + o_wcnt, *first = S + o_first, *tot = S + o_tot;
     run.long_total = lpos + n;
     run.giant_total = tot + 2;
-    run.sum_ctr = tot + 3;
+    run.sum_ctr = tot + 8;
     run.giant_pieces = tot + 5;
     const unsigned grid = ctx->sm_count * 4;
     // 1. row classes and the partition
@@ -1768,7 +1773,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
                                       run.work, run.long_count, run.giant_total, run.giant_pieces);
-    BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
+    BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 4 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
     k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, wcnt);
     BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
@@ -1799,6 +1804,21 @@ void free_run(PrRun &run, cudaStream_t s)
     run = PrRun{};
 }
 
+// The long-row sums of one iteration of the work-list variants.
+constexpr bool LONG_SUMS_SPLIT = false;
+template<bool NODIV>
+void launch_long_sums(bw_context *ctx, const PrArgs &a, cudaStream_t s)
+{
+    const unsigned grid = ctx->sm_count * LONG_SUM_BLOCKS_PER_SM;
+    if (LONG_SUMS_SPLIT) {
+        k_pr_long_sums<NODIV, 1><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        k_pr_long_sums<NODIV, 2><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        ctx->launches++;
+    } else {
+        k_pr_long_sums<NODIV, 0><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+    }
+}
+
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
 {
     switch (variant) {
@@ -1825,13 +1845,13 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
       case PR_VERTEX_PULL:
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        launch_long_sums<false>(ctx, a, s);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_NODIV:
         if (geo.block == PULL_WIDE) k_pr_pull_items<true, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<true, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        k_pr_long_sums<true><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        launch_long_sums<true>(ctx, a, s);
         ctx->launches++;
         break;
       case PR_VERTEX_PULL_WARP:
@@ -1850,7 +1870,7 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         // the vertex-pull kernel pair under the variant's own tuned shape
         if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
         else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        k_pr_long_sums<false><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+        launch_long_sums<false>(ctx, a, s);
         ctx->launches++;
         break;
       default: return BW_ERR_UNKNOWN_VARIANT;
