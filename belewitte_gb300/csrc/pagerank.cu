@@ -1507,10 +1507,7 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
 // giant row's combining piece resets the row's arrival counter.
 constexpr int LONG_SUM_THREADS = 256;
 constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
-// JOBS: 0 both job kinds (one launch), 1 the batches only, 2 the giant
-// rows' pieces only (two launches, each with its own counters: ctr[0..1]
-// and ctr[2..3]).
-template<bool NODIV, int JOBS>
+template<bool NODIV>
 __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr_long_sums(PrArgs a, uint32_t *ctr)
 {
     __shared__ __align__(16) float stage[LONG_SUM_THREADS / 32][33 * PIECE_L];
@@ -1518,13 +1515,12 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t L = *a.long_total, G = *a.giant_total, PG = *a.giant_pieces;
     const uint32_t MB = (L - G + 31) / 32;
-    const uint32_t first = JOBS == 2 ? MB : 0u, jobs = JOBS == 1 ? MB : MB + PG;
-    if (JOBS == 2) ctr += 2;
+    const uint32_t jobs = MB + PG;
     const float base_nd = nodiv_base(a.n);
     float dsum = 0.0f;
     for (;;) {
         uint32_t job = 0;
-        if (lane == 0) job = first + atomicAdd(&ctr[0], 1u);
+        if (lane == 0) job = atomicAdd(&ctr[0], 1u);
         job = __shfl_sync(FULL_MASK, job, 0);
         if (job >= jobs) break;
         if (job < MB) {
@@ -1773,7 +1769,7 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
                                       run.work, run.long_count, run.giant_total, run.giant_pieces);
-    BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 4 * sizeof(uint32_t), s));
+    BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
     k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, wcnt);
     BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
@@ -1805,18 +1801,10 @@ void free_run(PrRun &run, cudaStream_t s)
 }
 
 // The long-row sums of one iteration of the work-list variants.
-constexpr bool LONG_SUMS_SPLIT = false;
 template<bool NODIV>
-void launch_long_sums(bw_context *ctx, const PrArgs &a, cudaStream_t s)
+void launch_long_sums(const bw_context *ctx, const PrArgs &a, cudaStream_t s)
 {
-    const unsigned grid = ctx->sm_count * LONG_SUM_BLOCKS_PER_SM;
-    if (LONG_SUMS_SPLIT) {
-        k_pr_long_sums<NODIV, 1><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
-        k_pr_long_sums<NODIV, 2><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
-        ctx->launches++;
-    } else {
-        k_pr_long_sums<NODIV, 0><<<grid, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
-    }
+    k_pr_long_sums<NODIV><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
 }
 
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
