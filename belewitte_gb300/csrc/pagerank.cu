@@ -907,8 +907,9 @@ __global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint3
 // Exact long rows above GIANT_ROW terms are summed piece-parallel (binade
 // maps per piece, combined by the row's last piece); shorter ones in
 // batches of 32, one row per lane.  A lane's row is a chain of dependent
-// additions whose loads it can hold only a few dozen terms ahead: measured
-// on GB300 at about 29 cycles a term, which bounds the shorter rows' length.
+// additions with only a few dozen of its terms in flight (the warp's
+// shared-memory ring): the longest batch rows set the kernel's critical
+// path, which bounds their length.
 constexpr uint32_t GIANT_ROW = 2048;
 
 // Pieces of sorted long row i at [ppos[i], ppos[i + 1]); the arrival
@@ -1012,43 +1013,94 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
     }
 }
 
-// One lane's sequential float sum of p[0, len) -- the reference's row loop.
-// Four-term vector loads once aligned; the next 32 terms are in flight
-// while the current 32 are added (the data were written by the previous
-// kernel).
-__device__ __forceinline__ float lane_sequential_sum(const float *p, uint32_t len)
+// The batch rows of k_pr_long_sums: lane l returns the sequential float sum
+// of its row's terms vals[beg, beg + len), in row order.  A lane that reads
+// its own row strided from the others (one 16-byte load per lane and
+// instruction) keeps L1TEX on 32 lines per load: measured on GB300, about
+// 88 cycles a term.  Instead the warp stages its 32 rows through a ring of
+// BATCH_STAGES stages in shared memory with coalesced 16-byte cp.async
+// copies, issued BATCH_STAGES - 1 stages ahead.  Stage c of a row is the
+// 16-byte aligned window of BATCH_TERMS floats at (beg & ~3) + c *
+// BATCH_TERMS; window positions before beg or past the row's end add +0,
+// which leaves the running sum unchanged (it starts at +0 and is never -0:
+// x + -x rounds to +0), so the result is the plain loop's, bit for bit.
+// Chunks wholly past the row's end are zero-filled without a read; vals[]
+// holds 4 floats past the edges, the most a chunk that starts inside the
+// row reads beyond it.
+constexpr uint32_t BATCH_TERMS = 16;
+constexpr uint32_t BATCH_CHUNKS = BATCH_TERMS / 4;          // 16-byte chunks of a row per stage
+constexpr uint32_t BATCH_SLOT = BATCH_TERMS + 4;            // padded: conflict-free 16-byte reads
+constexpr uint32_t BATCH_STAGES = 3;
+constexpr uint32_t BATCH_RING = BATCH_STAGES * 32 * BATCH_SLOT;   // floats per warp
+static_assert(BATCH_TERMS % 4 == 0 && 32 % BATCH_CHUNKS == 0, "whole chunks; whole rows per copy");
+
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, uint32_t bytes)
 {
-    constexpr uint32_t Q = 12;                    // quads per stage (8: 1.5% slower on R-MAT-22)
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template<int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Out of line: its registers are allocated apart from the giant-row path's.
+__device__ __noinline__ float batch_sequential_sum(const float *vals, uint32_t beg, uint32_t len, float *ring,
+                                                   unsigned lane)
+{
+    constexpr uint32_t ROWS_PER_COPY = 32 / BATCH_CHUNKS;    // rows one copy instruction covers
+    constexpr uint32_t COPIES = 32 / ROWS_PER_COPY;          // copy instructions per stage
+    const uint32_t end = beg + len, a0 = beg & ~3u;
+    const uint32_t stages = (__reduce_max_sync(FULL_MASK, end - a0) + BATCH_TERMS - 1) / BATCH_TERMS;
+    // this lane copies chunk `k` of rows i * ROWS_PER_COPY + lane / BATCH_CHUNKS
+    const uint32_t k = lane % BATCH_CHUNKS;
+    uint32_t cg[COPIES], ce[COPIES];
+#pragma unroll
+    for (uint32_t i = 0; i < COPIES; i++) {
+        const uint32_t r = i * ROWS_PER_COPY + lane / BATCH_CHUNKS;
+        cg[i] = (__shfl_sync(FULL_MASK, beg, r) & ~3u) + 4 * k;
+        ce[i] = __shfl_sync(FULL_MASK, end, r);
+    }
+    auto issue = [&](uint32_t c) {
+        float *st = ring + (c % BATCH_STAGES) * (32 * BATCH_SLOT);
+#pragma unroll
+        for (uint32_t i = 0; i < COPIES; i++) {
+            const uint32_t r = i * ROWS_PER_COPY + lane / BATCH_CHUNKS, g = cg[i] + c * BATCH_TERMS;
+            const bool want = g < ce[i];
+            cp_async16(st + r * BATCH_SLOT + 4 * k, want ? vals + g : vals, want ? 16u : 0u);
+        }
+    };
+#pragma unroll 1
+    for (uint32_t c = 0; c + 1 < BATCH_STAGES; c++) {
+        if (c < stages) issue(c);
+        cp_async_commit();
+    }
     float acc = 0.0f;
-    uint32_t i = 0;
-    while (i < len && (reinterpret_cast<uintptr_t>(p + i) & 15)) acc = __fadd_rn(acc, __ldcg(p + i++));
-    const float4 *q = reinterpret_cast<const float4 *>(p + i);
-    const uint32_t quads = (len - i) / 4;
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 cur[Q];
+#pragma unroll 1
+    for (uint32_t c = 0; c < stages; c++) {
+        if (c + BATCH_STAGES - 1 < stages) issue(c + BATCH_STAGES - 1);
+        cp_async_commit();
+        cp_async_wait<BATCH_STAGES - 1>();           // this lane's copies of stage c are done
+        __syncwarp();                                // ... and every lane's
+        const float4 *mine = reinterpret_cast<const float4 *>(ring + (c % BATCH_STAGES) * (32 * BATCH_SLOT) +
+                                                              lane * BATCH_SLOT);
+        float x[BATCH_TERMS];
 #pragma unroll
-    for (uint32_t u = 0; u < Q; u++) cur[u] = u < quads ? __ldcg(q + u) : zero;
-    uint32_t k = 0;
-    for (; k + Q <= quads; k += Q) {
-        float4 nxt[Q];
-#pragma unroll
-        for (uint32_t u = 0; u < Q; u++) nxt[u] = k + Q + u < quads ? __ldcg(q + k + Q + u) : zero;
-#pragma unroll
-        for (uint32_t u = 0; u < Q; u++) {
-            acc = __fadd_rn(acc, cur[u].x); acc = __fadd_rn(acc, cur[u].y);
-            acc = __fadd_rn(acc, cur[u].z); acc = __fadd_rn(acc, cur[u].w);
+        for (uint32_t q = 0; q < BATCH_CHUNKS; q++) {
+            const float4 v = mine[q];
+            x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
         }
+        const uint32_t first = a0 + c * BATCH_TERMS;  // row position of the window's first float
+        if (first >= beg && first + BATCH_TERMS <= end) {
 #pragma unroll
-        for (uint32_t u = 0; u < Q; u++) cur[u] = nxt[u];
-    }
+            for (uint32_t t = 0; t < BATCH_TERMS; t++) acc = __fadd_rn(acc, x[t]);
+        } else {
 #pragma unroll
-    for (uint32_t u = 0; u + 1 < Q; u++) {        // the last 0-7 whole quads are in cur[]
-        if (k + u < quads) {
-            acc = __fadd_rn(acc, cur[u].x); acc = __fadd_rn(acc, cur[u].y);
-            acc = __fadd_rn(acc, cur[u].z); acc = __fadd_rn(acc, cur[u].w);
+            for (uint32_t t = 0; t < BATCH_TERMS; t++)
+                acc = __fadd_rn(acc, first + t >= beg && first + t < end ? x[t] : 0.0f);
         }
+        __syncwarp();                                // the slot is free for stage c + BATCH_STAGES
     }
-    for (i += quads * 4; i < len; i++) acc = __fadd_rn(acc, __ldcg(p + i));
+    cp_async_wait<0>();
     return acc;
 }
 
@@ -1487,7 +1539,7 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
 // are taken in order from a counter (no static share, so a warp that drew a
 // long job takes fewer):
 //  * first batches of 32 long rows of at most GIANT_ROW terms and similar
-//    length, one row per lane (lane_sequential_sum): the longest chains of
+//    length, one row per lane (batch_sequential_sum): the longest chains of
 //    dependent additions start first.
 //  * then the pieces of the rows above GIANT_ROW terms, longest rows
 //    first.  Piece 0 adds the row's first SERIAL_TERMS terms in order (one
@@ -1506,13 +1558,17 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
 // warp to finish resets the job counters for the next iteration; each
 // giant row's combining piece resets the row's arrival counter.
 constexpr int LONG_SUM_THREADS = 256;
-constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128 (3 spills)
+constexpr int LONG_SUM_BLOCKS_PER_SM = 2;            // registers <= 128
+constexpr uint32_t LONG_SUM_WARP_SMEM = BATCH_RING > 33 * PIECE_L ? BATCH_RING : 33 * PIECE_L;   // floats
+constexpr size_t LONG_SUM_SMEM = (LONG_SUM_THREADS / 32) * LONG_SUM_WARP_SMEM * sizeof(float);
 template<bool NODIV>
 __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr_long_sums(PrArgs a, uint32_t *ctr)
 {
-    __shared__ __align__(16) float stage[LONG_SUM_THREADS / 32][33 * PIECE_L];
+    extern __shared__ __align__(16) float long_smem[];   // per warp: the batch ring or a piece's stage
     resolve_args(a);
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float *const ring = long_smem + wib * LONG_SUM_WARP_SMEM;
+    float *const stage_w = ring;
     const uint32_t L = *a.long_total, G = *a.giant_total, PG = *a.giant_pieces;
     const uint32_t MB = (L - G + 31) / 32;
     const uint32_t jobs = MB + PG;
@@ -1525,13 +1581,16 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr
         if (job >= jobs) break;
         if (job < MB) {
             const uint32_t k = G + job * 32 + lane;
+            uint32_t row = 0, beg = 0, len = 0;
+            FinishIn fin{0.0f, 0u, 0u};
             if (k < L) {
-                const uint32_t row = a.long_rows[k];
-                const FinishIn fin = finish_load<NODIV>(a, row);
-                const uint32_t beg = a.rev_v[row];
-                const float sum = lane_sequential_sum(a.vals + beg, a.rev_v[row + 1] - beg);
-                dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
+                row = a.long_rows[k];
+                fin = finish_load<NODIV>(a, row);
+                beg = a.rev_v[row];
+                len = a.rev_v[row + 1] - beg;
             }
+            const float sum = batch_sequential_sum(a.vals, beg, len, ring, lane);
+            if (k < L) dsum += finish_store<NODIV>(a, row, sum, base_nd, fin);
         } else {
             job -= MB;
             const uint4 w = a.work[job];
@@ -1540,9 +1599,9 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr
             const float *rv = a.vals + beg;
             uint4 r0 = make_uint4(REC_NONE, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
             if (q == 0) {
-                r0 = make_uint4(REC_STATE, warp_serial_start(rv, stage[wib], lane), 0u, 0u);
+                r0 = make_uint4(REC_STATE, warp_serial_start(rv, stage_w, lane), 0u, 0u);
             } else if (q >= SERIAL_PIECES) {
-                piece_record(a, rv, n, p0, q, stage[wib], lane, r0, r1);
+                piece_record(a, rv, n, p0, q, stage_w, lane, r0, r1);
             }
             uint32_t last = 0;
             if (lane == 0) {
@@ -1552,7 +1611,7 @@ __global__ void __launch_bounds__(LONG_SUM_THREADS, LONG_SUM_BLOCKS_PER_SM) k_pr
             }
             if (__shfl_sync(FULL_MASK, last, 0)) {
                 __syncwarp();                         // orders every lane's reads after lane 0's acquire
-                const float total = combine_pieces(a, rv, n, p0, pieces, stage[wib], lane);
+                const float total = combine_pieces(a, rv, n, p0, pieces, stage_w, lane);
                 if (lane == 0) {
                     dsum += finish_vertex<NODIV>(a, row, total, base_nd);
                     a.long_count[row] = 0;
@@ -1780,7 +1839,8 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     run.count_nonconst = tot;
     run.count_all = tot + 1;
     if (m) {
-        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), m * sizeof(float), s));
+        // 4 floats past the edges: the batch sums' 16-byte copies (k_pr_long_sums)
+        BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.vals), (m + 4) * sizeof(float), s));
         const uint64_t pcap = m / SEG_EDGES + lcap + 1;     // pieces at most
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_map), 2 * pcap * sizeof(uint4), s));
         BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.piece_sum), pcap * sizeof(float), s));
@@ -1804,7 +1864,7 @@ void free_run(PrRun &run, cudaStream_t s)
 template<bool NODIV>
 void launch_long_sums(const bw_context *ctx, const PrArgs &a, cudaStream_t s)
 {
-    k_pr_long_sums<NODIV><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, 0, s>>>(a, a.sum_ctr);
+    k_pr_long_sums<NODIV><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, LONG_SUM_SMEM, s>>>(a, a.sum_ctr);
 }
 
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
@@ -2032,6 +2092,10 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     a.acc = ctx->pr_acc;
     a.gat_e = g->rev_edges;
     if (need_exact) {
+        BW_CUDA(cudaFuncSetAttribute(k_pr_long_sums<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(LONG_SUM_SMEM)));
+        BW_CUDA(cudaFuncSetAttribute(k_pr_long_sums<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(LONG_SUM_SMEM)));
         // hub cache entries per block: chunk_size when given, else the
         // default for the shape; never more than the block's share of
         // shared memory allows
