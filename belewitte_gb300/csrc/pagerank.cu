@@ -1324,8 +1324,13 @@ __device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, u
         const uint32_t k = u * 32 + lane;
         v[u] = k < len ? __ldcg(rv + b + k) : 0.0f;
     }
-    constexpr uint32_t PRE_U = 4;                    // the guess: earlier pieces' sums in double
-    double pre = 0.0;
+    // The guess: the earlier pieces' sums added in float.  Its error (a few
+    // ulps) is far below the sequential sum's own drift from the exact sum,
+    // and a guess off the true running sum's binade only sends the piece
+    // to exact evaluation.  (Adding in double cost more: GB300's FP64 pipe
+    // is narrow, and every piece adds all the sums before it.)
+    constexpr uint32_t PRE_U = 4;
+    float pre = 0.0f;
     for (uint32_t i0 = 0; i0 < q; i0 += 32 * PRE_U) {
         float f[PRE_U];
 #pragma unroll
@@ -1334,7 +1339,7 @@ __device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, u
             f[k] = i < q ? __ldcg(a.piece_sum + p0 + i) : 0.0f;
         }
 #pragma unroll
-        for (uint32_t k = 0; k < PRE_U; k++) pre += static_cast<double>(f[k]);
+        for (uint32_t k = 0; k < PRE_U; k++) pre += f[k];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(FULL_MASK, pre, o);   // same bits in every lane
@@ -1349,7 +1354,7 @@ __device__ __forceinline__ void piece_record(const PrArgs &a, const float *rv, u
         x[u] = __float_as_uint(stage[k + (k >> 5)]);   // past the end: +0, the identity
     }
     __syncwarp();
-    const uint32_t guess = __float_as_uint(__double2float_rn(pre));
+    const uint32_t guess = __float_as_uint(pre);
     record_of_terms(x, guess, lane, r0, r1);
 }
 
@@ -1544,7 +1549,7 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
 //  * then the pieces of the rows above GIANT_ROW terms, longest rows
 //    first.  Piece 0 adds the row's first SERIAL_TERMS terms in order (one
 //    lane, from shared memory).  Every later piece guesses the running sum at its start (the
-//    float sums of the pieces before it, added in double) and records, in
+//    float sums of the pieces before it, added in float) and records, in
 //    the guessed binade, the map of its terms -- or, when the guess crosses
 //    into the next binade inside the piece, the map of the terms before the
 //    crossing term, that term, and the map of the terms after it in the new
