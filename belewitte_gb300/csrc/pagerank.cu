@@ -22,12 +22,12 @@
 #include <cmath>
 #include <cstring>
 #include <cooperative_groups.h>
-#include <cub/cub.cuh>
 
 #include "bw_consolidate.h"
 #include "bw_seqsum.h"
 #include "bw_seqsum_warp.cuh"
 #include "bw_internal.cuh"
+#include "bw_sort.cuh"
 
 namespace bw {
 namespace {
@@ -105,6 +105,12 @@ struct PrArgs {
     const uint32_t *count_dev;    // work-list length (nullptr: work_count)
     const float *gat_in;
     float *gat_out;
+    // First iteration of a div work-list run in the hub-first order: the
+    // sources are read as vertex ids (rev_e) and translated by that
+    // iteration's kernel, which gathers {slot, first contribution} from
+    // first_pk and writes the slots to gat_e_out (nullptr: gat_e is ready).
+    const uint2 *first_pk;
+    uint32_t *gat_e_out;
     // Forward edge lists: the destination stream with the hot destinations
     // (the most edges in) replaced by HOT_BIT | their slot, and the vertex
     // of each slot (k_pr_edge_hot); nullptr: not built.
@@ -234,15 +240,21 @@ __global__ void k_pr_init(PrArgs a, float *pr, float *contrib, float *gat, int r
 // Storing the gathered array in decreasing out-degree order packs the hubs
 // of skewed graphs into few cache lines, which then stay in L1.  Rows keep
 // their order and their sources' order, so every sum is unchanged.
-__global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint64_t n, uint32_t *__restrict__ keys,
-                               uint32_t *__restrict__ ids)
-{
-    for (uint64_t v = gtid(); v < n; v += gthreads()) {
+// The sort key of a vertex: floor(log2(deg)) classes, larger degrees first
+// (32 for a vertex without out-edges).
+struct RelabelDigit {
+    const uint32_t *deg;
+    __device__ __forceinline__ uint32_t digit(uint64_t v) const
+    {
         const uint32_t d = deg[v];
-        keys[v] = d ? static_cast<uint32_t>(__clz(d)) : 32u;   // larger degree, smaller key
-        ids[v] = static_cast<uint32_t>(v);
+        return d ? static_cast<uint32_t>(__clz(d)) : 32u;
     }
-}
+};
+struct RelabelPut {
+    uint32_t *order;            // position -> vertex
+    __device__ __forceinline__ void put(uint32_t pos, uint64_t v) const { order[pos] = static_cast<uint32_t>(v); }
+};
+constexpr int RELABEL_BINS = 64, RELABEL_WARPS = 8;
 
 // Edges covered by the first `k` entries in degree order and in vertex
 // order (one block).
@@ -269,11 +281,22 @@ __global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint3
     }
 }
 
+// slot[v]; with pk, also {slot, first-iteration contribution} of each
+// vertex, the value k_pr_init gives the div variants (1/N over the degree).
 __global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, const uint32_t *on,
-                                uint32_t *__restrict__ slot)
+                                uint32_t *__restrict__ slot, const uint32_t *__restrict__ deg,
+                                uint2 *__restrict__ pk)
 {
     if (*on == 0) return;
-    for (uint64_t i = gtid(); i < n; i += gthreads()) slot[order[i]] = static_cast<uint32_t>(i);
+    const float init = __fdiv_rn(1.0f, static_cast<float>(n));
+    for (uint64_t i = gtid(); i < n; i += gthreads()) {
+        const uint32_t v = order[i];
+        slot[v] = static_cast<uint32_t>(i);
+        if (pk) {
+            const uint32_t d = deg[v];
+            pk[v] = make_uint2(static_cast<uint32_t>(i), __float_as_uint(d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f));
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) k_relabel_edges(const uint32_t *__restrict__ src, uint64_t m,
@@ -868,29 +891,76 @@ constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 //    and cut into SEG_EDGES pieces in that order, at the front of the list.
 // Layout: [pieces | short items | CONST items]; the lengths stay on the
 // device (tot[0] = items before the CONST ones, tot[1] = all items).
-__global__ void k_row_flags(const uint32_t *__restrict__ off, uint64_t n, uint32_t seg_long,
-                            uint32_t *__restrict__ flag, uint32_t *__restrict__ long_flag)
+// Tile b of SCAN_TILE rows: part_e[b] rows with in-edges, part_l[b] long rows.
+constexpr uint64_t ROW_TILE = sortk::SCAN_TILE;
+__global__ void __launch_bounds__(sortk::SCAN_THREADS) k_rows_count(const uint32_t *__restrict__ off, uint64_t n,
+                                                                    uint32_t seg_long, uint32_t *__restrict__ part_e,
+                                                                    uint32_t *__restrict__ part_l)
 {
-    for (uint64_t r = gtid(); r < n; r += gthreads()) {
-        const uint32_t d = off[r + 1] - off[r];
-        flag[r] = d ? 1u : 0u;
-        long_flag[r] = d > seg_long ? 1u : 0u;
+    __shared__ uint32_t ws[sortk::SCAN_THREADS / 32];
+    const uint64_t t0 = blockIdx.x * ROW_TILE;
+    uint32_t e = 0, l = 0;
+#pragma unroll
+    for (int k = 0; k < sortk::SCAN_ITEMS; k++) {
+        const uint64_t r = t0 + k * sortk::SCAN_THREADS + threadIdx.x;
+        if (r < n) {
+            const uint32_t d = off[r + 1] - off[r];
+            e += d ? 1u : 0u;
+            l += d > seg_long ? 1u : 0u;
+        }
+    }
+    uint32_t te, tl;
+    sortk::block_exclusive<sortk::SCAN_THREADS>(e, te, ws);
+    sortk::block_exclusive<sortk::SCAN_THREADS>(l, tl, ws);
+    if (threadIdx.x == 0) {
+        part_e[blockIdx.x] = te;
+        part_l[blockIdx.x] = tl;
     }
 }
 
-__global__ void k_row_partition(const uint32_t *__restrict__ off, uint64_t n, uint32_t seg_long,
-                                const uint32_t *__restrict__ pos,
-                                const uint32_t *__restrict__ long_pos, uint32_t *__restrict__ rows,
-                                uint32_t *__restrict__ long_len, uint32_t *__restrict__ long_row)
+// The stable partition, from the scanned tile counts (part_e[tiles] = ne
+// rows with in-edges, part_l[tiles] = long rows): rows with in-edges in row
+// order at rows[0, ne), the rest at rows[ne, n); the long rows, in row
+// order, with their lengths.  Each thread takes SCAN_ITEMS consecutive rows
+// of its tile, whose lengths are staged in shared memory.
+__global__ void __launch_bounds__(sortk::SCAN_THREADS) k_rows_partition(
+    const uint32_t *__restrict__ off, uint64_t n, uint32_t seg_long, const uint32_t *__restrict__ part_e,
+    const uint32_t *__restrict__ part_l, uint64_t tiles, uint32_t *__restrict__ rows,
+    uint32_t *__restrict__ long_len, uint32_t *__restrict__ long_row)
 {
-    const uint64_t ne = pos[n];
-    for (uint64_t r = gtid(); r < n; r += gthreads()) {
-        const uint32_t d = off[r + 1] - off[r];
-        if (d) rows[pos[r]] = static_cast<uint32_t>(r);
-        else rows[ne + (r - pos[r])] = static_cast<uint32_t>(r);
+    __shared__ uint32_t len[ROW_TILE + ROW_TILE / 32];
+    __shared__ uint32_t ws[sortk::SCAN_THREADS / 32];
+    const uint64_t t0 = blockIdx.x * ROW_TILE;
+#pragma unroll
+    for (int k = 0; k < sortk::SCAN_ITEMS; k++) {
+        const uint32_t j = k * sortk::SCAN_THREADS + threadIdx.x;
+        const uint64_t r = t0 + j;
+        len[sortk::scan_pad(j)] = r < n ? off[r + 1] - off[r] : 0u;
+    }
+    __syncthreads();
+    const uint32_t j0 = threadIdx.x * sortk::SCAN_ITEMS;
+    uint32_t e = 0, l = 0;
+#pragma unroll
+    for (int k = 0; k < sortk::SCAN_ITEMS; k++) {
+        const uint32_t d = len[sortk::scan_pad(j0 + k)];
+        e += d ? 1u : 0u;
+        l += d > seg_long ? 1u : 0u;
+    }
+    uint32_t te, tl;
+    uint32_t pe = part_e[blockIdx.x] + sortk::block_exclusive<sortk::SCAN_THREADS>(e, te, ws);
+    uint32_t pl = part_l[blockIdx.x] + sortk::block_exclusive<sortk::SCAN_THREADS>(l, tl, ws);
+    const uint64_t ne = part_e[tiles];
+    for (int k = 0; k < sortk::SCAN_ITEMS; k++) {
+        const uint64_t r = t0 + j0 + k;
+        if (r >= n) break;
+        const uint32_t d = len[sortk::scan_pad(j0 + k)];
+        // pe: rows with in-edges before r, so r - pe rows without
+        if (d) rows[pe++] = static_cast<uint32_t>(r);
+        else rows[ne + (r - pe)] = static_cast<uint32_t>(r);
         if (d > seg_long) {
-            long_len[long_pos[r]] = d;
-            long_row[long_pos[r]] = static_cast<uint32_t>(r);
+            long_len[pl] = d;
+            long_row[pl] = static_cast<uint32_t>(r);
+            pl++;
         }
     }
 }
@@ -911,6 +981,38 @@ __global__ void k_piece_count(const uint32_t *__restrict__ long_len, const uint3
 // shared-memory ring): the longest batch rows set the kernel's critical
 // path, which bounds their length.
 constexpr uint32_t GIANT_ROW = 2048;
+
+// Long rows are put in decreasing length order by one stable counting sort
+// on this key (smaller key, earlier row).  Rows of at most GIANT_ROW terms
+// (the batch rows) get one key per length, so their order is exact: rows of
+// equal length in row order.  The giant rows come first, in 64 classes per
+// octave of length (1.1% wide), each class in row order: their order only
+// schedules their pieces.
+constexpr uint32_t LONG_GIANT_KEYS = (32 - 11) * 64;                       // octaves 2^11 .. 2^31
+constexpr int LONG_SORT_BINS = 4096, LONG_SORT_WARPS = 4, LONG_SORT_GRID = 64;
+static_assert(LONG_GIANT_KEYS + GIANT_ROW <= LONG_SORT_BINS, "every key is a bin");
+__device__ __forceinline__ uint32_t long_row_key(uint32_t len)
+{
+    if (len > GIANT_ROW) {
+        const uint32_t b = 31u - static_cast<uint32_t>(__clz(len));              // 11 .. 31
+        const uint32_t cls = (b - 11u) * 64u + ((len >> (b - 6u)) & 63u);      // grows with len
+        return LONG_GIANT_KEYS - 1u - cls;
+    }
+    return LONG_GIANT_KEYS + (GIANT_ROW - len);
+}
+struct LongRowDigit {
+    const uint32_t *len;
+    __device__ __forceinline__ uint32_t digit(uint64_t i) const { return long_row_key(len[i]); }
+};
+struct LongRowPut {
+    const uint32_t *len_in, *row_in;
+    uint32_t *len_out, *row_out;
+    __device__ __forceinline__ void put(uint32_t pos, uint64_t i) const
+    {
+        len_out[pos] = len_in[i];
+        row_out[pos] = row_in[i];
+    }
+};
 
 // Pieces of sorted long row i at [ppos[i], ppos[i + 1]); the arrival
 // counters cleared; the number of rows above GIANT_ROW and of their pieces.
@@ -942,10 +1044,10 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
 // One thread per window of 32 rows of rows[0, ne): the short items it emits
 // (counts[w]); counts[W + w]: the CONST item of window w of rows[ne, N).
 __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                            const uint32_t *__restrict__ pos, uint64_t n, uint32_t seg_long,
+                            const uint32_t *__restrict__ ne_dev, uint64_t n, uint32_t seg_long,
                             uint32_t *__restrict__ counts)
 {
-    const uint64_t windows = (n + 31) / 32, ne = pos[n];
+    const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
     for (uint64_t w = gtid(); w < windows; w += gthreads()) {
         const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
         uint32_t items = 0, acc_edges = 0, acc_rows = 0;
@@ -969,12 +1071,12 @@ __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__
 // contiguous: rows in between have none); CONST items
 // {ne + k0, ne + k1 | CONST, 0, 0}; both after the P pieces.
 __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                           const uint32_t *__restrict__ pos, uint64_t n, uint32_t seg_long,
+                           const uint32_t *__restrict__ ne_dev, uint64_t n, uint32_t seg_long,
                            const uint32_t *__restrict__ first,
                            const uint32_t *__restrict__ piece_total, uint4 *__restrict__ work,
                            uint32_t *__restrict__ tot)
 {
-    const uint64_t windows = (n + 31) / 32, ne = pos[n];
+    const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
     const uint32_t P = *piece_total;
     if (gtid() == 0) {
         tot[0] = P + first[windows];
@@ -1114,10 +1216,23 @@ __device__ __forceinline__ float gather1(const float *__restrict__ src, const fl
     return i < hubs ? hub[i] : __ldcg(src + i);
 }
 
-// Gather src[rev_e[e0 + k]] for k in [0, len) (len <= SEG_EDGES) into buf.
+// The first iteration's value of source vertex i at edge e, whose slot it
+// writes to gat_out[e] (the translated source stream of later iterations).
+__device__ __forceinline__ float gather_first(const uint2 *__restrict__ pk, uint32_t *__restrict__ gat_out,
+                                              uint32_t i, uint32_t e)
+{
+    const uint2 p = __ldcg(pk + i);
+    __stcs(gat_out + e, p.x);
+    return __uint_as_float(p.y);
+}
+
+// Gather src[rev_e[e0 + k]] for k in [0, len) (len <= SEG_EDGES) into buf
+// (FIRST with pk: the first iteration's values and translation).
+template<bool FIRST>
 __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, const float *__restrict__ src,
                                             const float *hub, uint32_t hubs,
-                                            uint32_t e0, uint32_t len, float *buf, unsigned lane)
+                                            uint32_t e0, uint32_t len, float *buf, unsigned lane,
+                                            const uint2 *pk, uint32_t *gat_out)
 {
     for (uint32_t base = 0; base < len; base += 32 * GATHER_UNROLL) {
         uint32_t idx[GATHER_UNROLL];
@@ -1130,7 +1245,8 @@ __device__ __forceinline__ void gather_into(const uint32_t *__restrict__ rev_e, 
 #pragma unroll
         for (int u = 0; u < GATHER_UNROLL; u++) {
             const uint32_t k = base + u * 32 + lane;
-            v[u] = k < len ? gather1(src, hub, hubs, idx[u]) : 0.0f;
+            if (FIRST && pk) v[u] = k < len ? gather_first(pk, gat_out, idx[u], e0 + k) : 0.0f;
+            else v[u] = k < len ? gather1(src, hub, hubs, idx[u]) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < GATHER_UNROLL; u++) {
@@ -1458,7 +1574,9 @@ __device__ __forceinline__ float combine_pieces(const PrArgs &a, const float *rv
 }
 
 
-template<bool NODIV, int BLOCK>
+// FIRST: the div variants' first iteration, which also translates the
+// sources when the hub-first order was taken (first_pk; no hub cache then).
+template<bool NODIV, int BLOCK, bool FIRST = false>
 __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items(PrArgs a)
 {
     constexpr int PULL_WARPS = BLOCK / 32;
@@ -1467,12 +1585,14 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
     const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = gtid() >> 5, warps = gthreads() >> 5;
     const float *src = NODIV ? (a.gat_in ? a.gat_in : a.pr_in) : a.contrib_in;
-    const uint32_t *ge = a.gat_e;
+    const uint2 *pk = (FIRST && a.slot) ? a.first_pk : nullptr;
+    uint32_t *const gat_out = a.gat_e_out;
+    const uint32_t *ge = pk ? a.rev_e : a.gat_e;
     const float base_nd = nodiv_base(a.n);
     float *buf = smem_f + wib * PULL_BUF;
     uint32_t *s_end = reinterpret_cast<uint32_t *>(smem_f + PULL_WARPS * PULL_BUF) + wib * 33;
     float *hub = smem_f + PULL_WARPS * (PULL_BUF + 33);
-    const uint32_t hubs = a.hub_count;       // multiple of 4
+    const uint32_t hubs = pk ? 0u : a.hub_count;       // multiple of 4
     for (uint32_t i = threadIdx.x; i < hubs / 4; i += blockDim.x)
         reinterpret_cast<float4 *>(hub)[i] = __ldg(reinterpret_cast<const float4 *>(src) + i);
     __syncthreads();
@@ -1501,7 +1621,8 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
                 for (int u = 0; u < GATHER_UNROLL; u++) {
                     const uint32_t k = base + u * 32 + lane;
                     if (k < len) {
-                        const float v = gather1(src, hub, hubs, idx[u]);
+                        const float v = (FIRST && pk) ? gather_first(pk, gat_out, idx[u], e0 + k)
+                                                      : gather1(src, hub, hubs, idx[u]);
                         __stcg(a.vals + e0 + k, v);
                         part += v;
                     }
@@ -1525,7 +1646,7 @@ __global__ void __launch_bounds__(BLOCK, pull_min_blocks(BLOCK)) k_pr_pull_items
             continue;
         }
         if (lane < rows) s_end[lane] = a.rev_v[row + 1] - e0;
-        gather_into(ge, src, hub, hubs, e0, len, buf, lane);
+        gather_into<FIRST>(ge, src, hub, hubs, e0, len, buf, lane, pk, gat_out);
         __syncwarp();
         if (lane < rows) {
             const uint32_t b = lane ? s_end[lane - 1] : 0u, e = s_end[lane];
@@ -1775,23 +1896,12 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     const uint64_t lcap = m / (seg_long + 1) + 1;          // long rows at most
     // Pieces <= M / SEG_EDGES + lcap; short items <= N + W; CONST <= W.
     const uint64_t cap = 2 * windows + n + m / SEG_EDGES + lcap + 16;
-    size_t t_scan_n = 0, t_scan_l = 0, t_scan_w = 0, t_sort = 0;
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_n, static_cast<uint32_t *>(nullptr),
-                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(n + 1), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_l, static_cast<uint32_t *>(nullptr),
-                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(lcap + 1), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan_w, static_cast<uint32_t *>(nullptr),
-                                          static_cast<uint32_t *>(nullptr), static_cast<int64_t>(2 * windows + 1), s));
-    cub::DoubleBuffer<uint32_t> lkeys(nullptr, nullptr), lids(nullptr, nullptr);
-    BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(nullptr, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
-    const size_t temp = std::max(std::max(t_scan_n, t_scan_l), std::max(t_scan_w, t_sort));
+    const uint64_t tiles = (n + ROW_TILE - 1) / ROW_TILE;
     // one allocation, 256-byte aligned regions (sizes in words)
     auto al = [](uint64_t w) { return (w + 63) & ~uint64_t(63); };
     uint64_t at = 0;
-    const uint64_t o_flag = at; at += al(n + 1);
-    const uint64_t o_pos = at; at += al(n + 1);
-    const uint64_t o_lflag = at; at += al(n + 1);
-    const uint64_t o_lpos = at; at += al(n + 1);
+    const uint64_t o_pe = at; at += al(tiles + 1);
+    const uint64_t o_pl = at; at += al(tiles + 1);
     const uint64_t o_lkey0 = at; at += al(lcap);
     const uint64_t o_lkey1 = at; at += al(lcap);
     const uint64_t o_lid0 = at; at += al(lcap);
@@ -1801,45 +1911,48 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     const uint64_t o_wcnt = at; at += al(2 * windows + 1);
     const uint64_t o_first = at; at += al(2 * windows + 1);
     const uint64_t o_tot = at; at += al(12);   // lengths, giant rows, long-sum counters (tot + 8)
-    const uint64_t o_temp = at;
-    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.scratch), o_temp * sizeof(uint32_t) + temp, s));
+    const uint64_t o_sort = at; at += al(sortk::digit_sort_words<LONG_SORT_BINS>(LONG_SORT_GRID));
+    const uint64_t o_part = at; at += al(std::max(sortk::scan_parts(lcap + 1), sortk::scan_parts(2 * windows + 1)));
+    BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.scratch), at * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.work), cap * sizeof(uint4), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.long_count), n * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&run.rows), n * sizeof(uint32_t), s));
     uint32_t *S = run.scratch;
-    void *tmp = S + o_temp;
-    uint32_t *flag = S + o_flag, *pos = S + o_pos, *lflag = S + o_lflag, *lpos = S + o_lpos;
+    uint32_t *part_e = S + o_pe, *part_l = S + o_pl, *part = S + o_part;
     uint32_t *pcnt = S + o_pcnt, *ppos = S + o_ppos, *wcnt = S + o_wcnt, *first = S + o_first, *tot = S + o_tot;
-    run.long_total = lpos + n;
+    const uint32_t *ne = part_e + tiles;
+    run.long_total = part_l + tiles;
     run.giant_total = tot + 2;
     run.sum_ctr = tot + 8;
     run.giant_pieces = tot + 5;
     const unsigned grid = ctx->sm_count * 4;
-    // 1. row classes and the partition
-    k_row_flags<<<grid, 256, 0, s>>>(g->rev_vertices, n, seg_long, flag, lflag);
-    BW_CUDA(cudaMemsetAsync(flag + n, 0, sizeof(uint32_t), s));
-    BW_CUDA(cudaMemsetAsync(lflag + n, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, flag, pos, static_cast<int64_t>(n + 1), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_n, lflag, lpos, static_cast<int64_t>(n + 1), s));
-    BW_CUDA(cudaMemsetAsync(S + o_lkey0, 0, lcap * sizeof(uint32_t), s));   // past the last long row: length 0
-    k_row_partition<<<grid, 256, 0, s>>>(g->rev_vertices, n, seg_long, pos, lpos, run.rows, S + o_lkey0, S + o_lid0);
-    // 2. long rows by decreasing length (stable), their pieces in that order
-    lkeys = cub::DoubleBuffer<uint32_t>(S + o_lkey0, S + o_lkey1);
-    lids = cub::DoubleBuffer<uint32_t>(S + o_lid0, S + o_lid1);
-    BW_CUDA(cub::DeviceRadixSort::SortPairsDescending(tmp, t_sort, lkeys, lids, static_cast<int64_t>(lcap), 0, 32, s));
-    run.long_rows = lids.Current();
-    k_piece_count<<<grid, 256, 0, s>>>(lkeys.Current(), run.long_total, lcap, pcnt);
+    // 1. the stable partition of the rows (with / without in-edges) and the
+    //    long rows in row order
+    k_rows_count<<<static_cast<unsigned>(tiles), sortk::SCAN_THREADS, 0, s>>>(g->rev_vertices, n, seg_long,
+                                                                             part_e, part_l);
+    sortk::k_scan_parts<<<1, 1024, 0, s>>>(part_e, tiles);
+    sortk::k_scan_parts<<<1, 1024, 0, s>>>(part_l, tiles);
+    k_rows_partition<<<static_cast<unsigned>(tiles), sortk::SCAN_THREADS, 0, s>>>(
+        g->rev_vertices, n, seg_long, part_e, part_l, tiles, run.rows, S + o_lkey0, S + o_lid0);
+    // 2. long rows by decreasing length (long_row_key), their pieces in that order
+    BW_CUDA((sortk::digit_sort<LONG_SORT_BINS, LONG_SORT_WARPS>(
+        LongRowDigit{S + o_lkey0}, LongRowPut{S + o_lkey0, S + o_lid0, S + o_lkey1, S + o_lid1}, lcap,
+        run.long_total, LONG_SORT_GRID, S + o_sort, s)));
+    const uint32_t *long_len = S + o_lkey1;
+    run.long_rows = S + o_lid1;
+    k_piece_count<<<grid, 256, 0, s>>>(long_len, run.long_total, lcap, pcnt);
     BW_CUDA(cudaMemsetAsync(pcnt + lcap, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_l, pcnt, ppos, static_cast<int64_t>(lcap + 1), s));
-    k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, lkeys.Current(), run.long_total, ppos,
+    BW_CUDA(sortk::scan_exclusive(pcnt, ppos, lcap + 1, part, s));
+    k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, long_len, run.long_total, ppos,
                                       run.work, run.long_count, run.giant_total, run.giant_pieces);
     BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
     // 3. short and CONST items after the pieces
-    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, wcnt);
+    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, wcnt);
     BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
-    BW_CUDA(cub::DeviceScan::ExclusiveSum(tmp, t_scan_w, wcnt, first, static_cast<int64_t>(2 * windows + 1), s));
-    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, pos, n, seg_long, first, ppos + lcap, run.work, tot);
-    ctx->launches += 6;                  // flags, partition, piece count/emit, count, emit (scans, sort: library)
+    BW_CUDA(sortk::scan_exclusive(wcnt, first, 2 * windows + 1, part, s));
+    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, first, ppos + lcap, run.work, tot);
+    // rows count/partition, two tile scans, sort 4, piece count/scan 3/emit, seg count/scan 3/emit
+    ctx->launches += 20;
     BW_CUDA(cudaGetLastError());
     run.count_nonconst = tot;
     run.count_all = tot + 1;
@@ -1872,6 +1985,20 @@ void launch_long_sums(const bw_context *ctx, const PrArgs &a, cudaStream_t s)
     k_pr_long_sums<NODIV><<<ctx->sm_count * LONG_SUM_BLOCKS_PER_SM, LONG_SUM_THREADS, LONG_SUM_SMEM, s>>>(a, a.sum_ctr);
 }
 
+// The work-list kernel of the div variants; the first iteration's instance
+// translates the sources when first_pk is set.
+void launch_pull_items_div(const PrArgs &a, const Geometry &geo, cudaStream_t s)
+{
+    const size_t smem = geo.smem + a.hub_count * 4;
+    if (geo.block == PULL_WIDE) {
+        if (a.first_pk) k_pr_pull_items<false, PULL_WIDE, true><<<geo.grid, geo.block, smem, s>>>(a);
+        else k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, smem, s>>>(a);
+    } else {
+        if (a.first_pk) k_pr_pull_items<false, PULL_NARROW, true><<<geo.grid, geo.block, smem, s>>>(a);
+        else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, smem, s>>>(a);
+    }
+}
+
 int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &geo, cudaStream_t s)
 {
     switch (variant) {
@@ -1896,8 +2023,7 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         ctx->launches++;
         break;
       case PR_VERTEX_PULL:
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        launch_pull_items_div(a, geo, s);
         launch_long_sums<false>(ctx, a, s);
         ctx->launches++;
         break;
@@ -1921,8 +2047,7 @@ int launch_iteration(bw_context *ctx, int variant, PrArgs &a, const Geometry &ge
         break;
       case PR_PULL_SEGMENTED:
         // the vertex-pull kernel pair under the variant's own tuned shape
-        if (geo.block == PULL_WIDE) k_pr_pull_items<false, PULL_WIDE><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
-        else k_pr_pull_items<false, PULL_NARROW><<<geo.grid, geo.block, geo.smem + a.hub_count * 4, s>>>(a);
+        launch_pull_items_div(a, geo, s);
         launch_long_sums<false>(ctx, a, s);
         ctx->launches++;
         break;
@@ -1942,6 +2067,8 @@ struct Relabel {
     uint32_t *slot = nullptr;     // vertex -> position in the gathered array
     uint32_t *gat_e = nullptr;    // reverse-CSR sources as positions
     uint32_t *on = nullptr;       // device: the order was taken
+    uint2 *pk = nullptr;          // div: {slot, first contribution} per vertex (the
+                                  // first iteration translates the sources)
     void *scratch = nullptr;
 };
 
@@ -1952,33 +2079,34 @@ struct Relabel {
 // would cover at least 5% more of the edges than in vertex order; the slot
 // and translation kernels, and every iteration, read that decision.
 int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, uint32_t hubs, bool force,
-                  Relabel &r, cudaStream_t s)
+                  bool first_translates, Relabel &r, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count, m = g->edge_count;
-    size_t temp = 0;
-    cub::DoubleBuffer<uint32_t> keys(nullptr, nullptr), ids(nullptr, nullptr);
-    BW_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
-    const size_t words = 4 * n, temp_words = (temp + 3) / 4;
-    const size_t on_at = words + temp_words;
-    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (on_at + 1) * sizeof(uint32_t), s));
+    const uint32_t grid = ctx->sm_count * 2;
+    const uint64_t order_words = (n + 63) & ~uint64_t(63);
+    const uint64_t sort_words = sortk::digit_sort_words<RELABEL_BINS>(grid);
+    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (order_words + sort_words + 1) * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
-    uint32_t *base = static_cast<uint32_t *>(r.scratch);
-    r.on = base + on_at;
-    keys = cub::DoubleBuffer<uint32_t>(base, base + n);
-    ids = cub::DoubleBuffer<uint32_t>(base + 2 * n, base + 3 * n);
-    k_relabel_keys<<<ctx->sm_count * 4, 256, 0, s>>>(deg, n, keys.Current(), ids.Current());
-    ctx->launches++;
-    BW_CUDA(cub::DeviceRadixSort::SortPairs(base + words, temp, keys, ids, static_cast<int64_t>(n), 0, 6, s));
+    uint32_t *order = static_cast<uint32_t *>(r.scratch);
+    r.on = order + order_words + sort_words;
+    // vertices by degree class, stable (one counting-sort pass)
+    BW_CUDA((sortk::digit_sort<RELABEL_BINS, RELABEL_WARPS>(RelabelDigit{deg}, RelabelPut{order}, n, nullptr, grid,
+                                                           order + order_words, s)));
+    ctx->launches += 5;                  // count, three scan launches, scatter
     if (force) {
         BW_CUDA(cudaMemsetAsync(r.on, 1, sizeof(uint32_t), s));
     } else {
-        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, ids.Current(), std::min<uint64_t>(hubs, n), m, r.on);
+        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, order, std::min<uint64_t>(hubs, n), m, r.on);
         ctx->launches++;
     }
-    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(ids.Current(), n, r.on, r.slot);
-    if (m) k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.on, r.slot, r.gat_e);
-    ctx->launches += m ? 2 : 1;
+    if (first_translates) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.pk), n * sizeof(uint2), s));
+    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(order, n, r.on, r.slot, deg, r.pk);
+    ctx->launches++;
+    if (m && !first_translates) {
+        k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.on, r.slot, r.gat_e);
+        ctx->launches++;
+    }
     BW_CUDA(cudaGetLastError());
     return BW_OK;
 }
@@ -1988,6 +2116,7 @@ void free_relabel(Relabel &r, cudaStream_t s)
     if (r.scratch) cudaFreeAsync(r.scratch, s);
     if (r.slot) cudaFreeAsync(r.slot, s);
     if (r.gat_e) cudaFreeAsync(r.gat_e, s);
+    if (r.pk) cudaFreeAsync(r.pk, s);
     r = Relabel{};
 }
 
@@ -2115,9 +2244,11 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         const int bytes = static_cast<int>(fixed + a.hub_count * sizeof(float));
         if (block == PULL_WIDE) {
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_WIDE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, PULL_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         } else {
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+            BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<false, PULL_NARROW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
             BW_CUDA(cudaFuncSetAttribute(k_pr_pull_items<true, PULL_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         }
     }
@@ -2143,7 +2274,8 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
     bool relabel = false;                 // may be taken (the device decides)
     if (all_items && g->edge_count > 0 && !(flags & BW_LAUNCH_NO_RELABEL) &&
         (force || (iterations >= 4 && a.hub_count > 0))) {
-        const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, rl, s);
+        // div: the first iteration translates the sources itself
+        const int rc = build_relabel(ctx, g, ctx->pr_deg, a.hub_count, force, !nodiv, rl, s);
         if (rc != BW_OK) {
             free_relabel(rl, s);
             free_run(exact_run, s);
@@ -2152,6 +2284,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         relabel = true;
         a.slot = rl.slot;
         a.gat_e = rl.gat_e;
+        a.gat_e_out = rl.gat_e;
         a.relabel_on = rl.on;
     }
     // forward edge lists: the hot destinations' slots and the rewritten
@@ -2251,6 +2384,7 @@ int run_pagerank(bw_context *ctx, const bw_graph_view *g, const int32_t *schedul
         if (time_iterations) BW_CUDA(cudaEventRecord(ctx->level_events[j - 1], ls));
         a.not_last = iterations > j ? 1 : 0;
         a.diff = ctx->pr_diffs + (j - 1);
+        a.first_pk = j == 1 ? rl.pk : nullptr;
         if (nodiv) {
             a.pr_in = nb[(j - 1) & 1];
             a.pr_out = nb[j & 1];
