@@ -250,22 +250,43 @@ struct RelabelDigit {
         return d ? static_cast<uint32_t>(__clz(d)) : 32u;
     }
 };
+// The sort's output, written per vertex v (coalesced: the sort walks the
+// vertices in order) and per position: order[pos] = v, slot[v] = pos and,
+// for the div variants, pk[v] = {pos, first-iteration contribution} -- the
+// value k_pr_init gives them, 1/N over the degree.  Written whether or not
+// the order is taken: nothing reads them unless it is.
 struct RelabelPut {
-    uint32_t *order;            // position -> vertex
-    __device__ __forceinline__ void put(uint32_t pos, uint64_t v) const { order[pos] = static_cast<uint32_t>(v); }
+    uint32_t *order, *slot;
+    uint2 *pk;
+    const uint32_t *deg;
+    float init;
+    __device__ __forceinline__ void put(uint32_t pos, uint64_t v) const
+    {
+        order[pos] = static_cast<uint32_t>(v);
+        slot[v] = pos;
+        if (pk) {
+            const uint32_t d = deg[v];
+            pk[v] = make_uint2(pos, __float_as_uint(d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f));
+        }
+    }
 };
-constexpr int RELABEL_BINS = 64, RELABEL_WARPS = 8;
+constexpr int RELABEL_BINS = 64, RELABEL_WARPS = 8, RELABEL_BLOCKS_PER_SM = 8;
 
-// Edges covered by the first `k` entries in degree order and in vertex
-// order (one block).
-__global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ order,
-                                   uint64_t k, uint64_t m, uint32_t *on)
+// Edges covered by the first `k` entries in degree order (cov[0]) and in
+// vertex order (cov[1]), from counters the caller zeroed; the last block to
+// finish (cov[2] counts them) decides whether the order is worth a pass over
+// the edges (>= 5% more of them on the cached hubs) and writes *on.
+__global__ void __launch_bounds__(1024) k_relabel_coverage(const uint32_t *__restrict__ deg,
+                                                           const uint32_t *__restrict__ order, uint64_t k,
+                                                           uint64_t m, unsigned long long *cov, uint32_t *on)
 {
     __shared__ unsigned long long part[2][32];
+    __shared__ bool last;
     unsigned long long sorted = 0, natural = 0;
-    for (uint64_t i = threadIdx.x; i < k; i += blockDim.x) {
-        sorted += deg[order[i]];
-        natural += deg[i];
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i < k) {
+        sorted = deg[order[i]];
+        natural = deg[i];
     }
     for (int o = 16; o > 0; o >>= 1) {
         sorted += __shfl_xor_sync(FULL_MASK, sorted, o);
@@ -276,26 +297,16 @@ __global__ void k_relabel_coverage(const uint32_t *__restrict__ deg, const uint3
     if (threadIdx.x == 0) {
         unsigned long long a = 0, b = 0;
         for (unsigned w = 0; w < blockDim.x / 32; w++) { a += part[0][w]; b += part[1][w]; }
-        // worth a pass over the edges: >= 5% more of them on the cached hubs
-        *on = (static_cast<double>(a) - static_cast<double>(b) >= 0.05 * static_cast<double>(m)) ? 1u : 0u;
+        atomicAdd(&cov[0], a);
+        atomicAdd(&cov[1], b);
+        __threadfence();
+        last = atomicAdd(reinterpret_cast<unsigned int *>(&cov[2]), 1u) + 1 == gridDim.x;
     }
-}
-
-// slot[v]; with pk, also {slot, first-iteration contribution} of each
-// vertex, the value k_pr_init gives the div variants (1/N over the degree).
-__global__ void k_relabel_slots(const uint32_t *__restrict__ order, uint64_t n, const uint32_t *on,
-                                uint32_t *__restrict__ slot, const uint32_t *__restrict__ deg,
-                                uint2 *__restrict__ pk)
-{
-    if (*on == 0) return;
-    const float init = __fdiv_rn(1.0f, static_cast<float>(n));
-    for (uint64_t i = gtid(); i < n; i += gthreads()) {
-        const uint32_t v = order[i];
-        slot[v] = static_cast<uint32_t>(i);
-        if (pk) {
-            const uint32_t d = deg[v];
-            pk[v] = make_uint2(static_cast<uint32_t>(i), __float_as_uint(d ? __fdiv_rn(init, static_cast<float>(d)) : 0.0f));
-        }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long a = atomicAdd(&cov[0], 0ull), b = atomicAdd(&cov[1], 0ull);
+        *on = (static_cast<double>(a) - static_cast<double>(b) >= 0.05 * static_cast<double>(m)) ? 1u : 0u;
     }
 }
 
@@ -1041,29 +1052,57 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
     }
 }
 
-// One thread per window of 32 rows of rows[0, ne): the short items it emits
-// (counts[w]); counts[W + w]: the CONST item of window w of rows[ne, N).
+// Short items are cut greedily over windows of 32 rows of rows[0, ne), in
+// order: an item ends before a long row (more than seg_long edges) and
+// before a row that would take it past SEG_EDGES edges.  One warp per
+// window: lane l loads row k0 + l (its length and first edge), then every
+// lane runs the same greedy walk over the shuffled lengths, so all lanes
+// hold the window's item starts and ends (bit l: an item starts at / ends
+// with row k0 + l).
+struct WindowRows {
+    uint32_t d, o;        // this lane's row: length, first edge
+    uint32_t starts, ends;
+};
+__device__ __forceinline__ WindowRows window_items(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
+                                                   uint64_t k0, uint64_t ne, uint32_t seg_long, unsigned lane)
+{
+    WindowRows w{0u, 0u, 0u, 0u};
+    const uint32_t cnt = k0 < ne ? static_cast<uint32_t>(ne - k0 < 32 ? ne - k0 : 32) : 0u;
+    if (lane < cnt) {
+        const uint32_t r = rows[k0 + lane];
+        w.o = off[r];
+        w.d = off[r + 1] - w.o;
+    }
+    uint32_t acc_e = 0, acc_r = 0;
+    for (uint32_t l = 0; l < cnt; l++) {
+        const uint32_t dl = __shfl_sync(FULL_MASK, w.d, l);
+        if (dl > seg_long) {                         // long rows go to pieces
+            if (acc_r) { w.ends |= 1u << (l - 1); acc_r = 0; acc_e = 0; }
+            continue;
+        }
+        if (acc_r && acc_e + dl > SEG_EDGES) { w.ends |= 1u << (l - 1); acc_r = 0; acc_e = 0; }
+        if (acc_r == 0) w.starts |= 1u << l;
+        acc_r++;
+        acc_e += dl;
+    }
+    if (acc_r) w.ends |= 1u << (cnt - 1);
+    return w;
+}
+
+// counts[w]: the short items of window w; counts[W + w]: the CONST item of
+// window w of rows[ne, N).
 __global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
                             const uint32_t *__restrict__ ne_dev, uint64_t n, uint32_t seg_long,
                             uint32_t *__restrict__ counts)
 {
     const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
-    for (uint64_t w = gtid(); w < windows; w += gthreads()) {
-        const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
-        uint32_t items = 0, acc_edges = 0, acc_rows = 0;
-        for (uint64_t k = k0; k < k1; k++) {
-            const uint32_t r = rows[k];
-            const uint32_t d = off[r + 1] - off[r];
-            if (d > seg_long) {                 // long rows go to pieces
-                if (acc_rows) { items++; acc_rows = 0; acc_edges = 0; }
-                continue;
-            }
-            if (acc_rows && acc_edges + d > SEG_EDGES) { items++; acc_rows = 0; acc_edges = 0; }
-            acc_rows++; acc_edges += d;
+    const unsigned lane = threadIdx.x & 31;
+    for (uint64_t w = gtid() >> 5; w < windows; w += gthreads() >> 5) {
+        const WindowRows wr = window_items(off, rows, w * 32, ne, seg_long, lane);
+        if (lane == 0) {
+            counts[w] = __popc(wr.starts);
+            counts[windows + w] = w * 32 < n - ne ? 1u : 0u;
         }
-        if (acc_rows) items++;
-        counts[w] = items;
-        counts[windows + w] = w * 32 < n - ne ? 1u : 0u;
     }
 }
 
@@ -1078,38 +1117,24 @@ __global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__r
 {
     const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
     const uint32_t P = *piece_total;
+    const unsigned lane = threadIdx.x & 31;
     if (gtid() == 0) {
         tot[0] = P + first[windows];
         tot[1] = P + first[2 * windows];
     }
-    for (uint64_t w = gtid(); w < windows; w += gthreads()) {
-        const uint64_t k0 = w * 32, k1 = min(ne, k0 + 32);
-        uint32_t out = P + first[w];
-        uint64_t start = k0;
-        uint32_t acc_edges = 0, acc_rows = 0;
-        for (uint64_t k = k0; k < k1; k++) {
-            const uint32_t r = rows[k];
-            const uint32_t d = off[r + 1] - off[r];
-            if (d > seg_long) {
-                if (acc_rows) {
-                    work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
-                    acc_rows = 0; acc_edges = 0;
-                }
-                continue;
-            }
-            if (acc_rows && acc_edges + d > SEG_EDGES) {
-                work[out++] = make_uint4(uint32_t(start), uint32_t(k), off[rows[start]], off[r]);
-                acc_rows = 0; acc_edges = 0;
-            }
-            if (acc_rows == 0) start = k;
-            acc_rows++; acc_edges += d;
-        }
-        if (acc_rows) {
-            const uint32_t last = rows[k1 - 1];
-            work[out++] = make_uint4(uint32_t(start), uint32_t(k1), off[rows[start]], off[last + 1]);
-        }
-        if (w * 32 < n - ne) {
-            const uint64_t c0 = ne + w * 32, c1 = min(n, c0 + 32);
+    for (uint64_t w = gtid() >> 5; w < windows; w += gthreads() >> 5) {
+        const uint64_t k0 = w * 32;
+        const WindowRows wr = window_items(off, rows, k0, ne, seg_long, lane);
+        // an item starting at this lane ends with the first end at or after it
+        const bool start = (wr.starts >> lane) & 1u;
+        const uint32_t below = (1u << lane) - 1u;
+        const uint32_t e = start ? static_cast<uint32_t>(__ffs(wr.ends & ~below) - 1) : lane;
+        const uint32_t oe = __shfl_sync(FULL_MASK, wr.o, e), de = __shfl_sync(FULL_MASK, wr.d, e);
+        if (start)
+            work[P + first[w] + __popc(wr.starts & below)] =
+                make_uint4(static_cast<uint32_t>(k0 + lane), static_cast<uint32_t>(k0 + e + 1), wr.o, oe + de);
+        if (lane == 0 && k0 < n - ne) {
+            const uint64_t c0 = ne + k0, c1 = min(n, c0 + 32);
             work[P + first[windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
         }
     }
@@ -2082,27 +2107,35 @@ int build_relabel(bw_context *ctx, const bw_graph_view *g, const uint32_t *deg, 
                   bool first_translates, Relabel &r, cudaStream_t s)
 {
     const uint64_t n = g->vertex_count, m = g->edge_count;
-    const uint32_t grid = ctx->sm_count * 2;
+    const uint32_t grid = ctx->sm_count * RELABEL_BLOCKS_PER_SM;
     const uint64_t order_words = (n + 63) & ~uint64_t(63);
-    const uint64_t sort_words = sortk::digit_sort_words<RELABEL_BINS>(grid);
-    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (order_words + sort_words + 1) * sizeof(uint32_t), s));
+    const uint64_t sort_words = (sortk::digit_sort_words<RELABEL_BINS>(grid) + 63) & ~uint64_t(63);
+    // order, the sort's scratch, three 64-bit coverage counters, the decision
+    BW_CUDA(ctx_malloc_async(ctx, &r.scratch, (order_words + sort_words + 8) * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.slot), n * sizeof(uint32_t), s));
     BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.gat_e), (m ? m : 1) * sizeof(uint32_t), s));
+    if (first_translates) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.pk), n * sizeof(uint2), s));
     uint32_t *order = static_cast<uint32_t *>(r.scratch);
-    r.on = order + order_words + sort_words;
-    // vertices by degree class, stable (one counting-sort pass)
-    BW_CUDA((sortk::digit_sort<RELABEL_BINS, RELABEL_WARPS>(RelabelDigit{deg}, RelabelPut{order}, n, nullptr, grid,
-                                                           order + order_words, s)));
+    auto *cov = reinterpret_cast<unsigned long long *>(order + order_words + sort_words);
+    r.on = order + order_words + sort_words + 6;
+    // vertices by degree class, stable (one counting-sort pass), with their
+    // slots (and first-iteration entries) written by the sort itself
+    const float init = 1.0f / static_cast<float>(n);        // k_pr_init's 1/N, IEEE single
+    BW_CUDA((sortk::digit_sort<RELABEL_BINS, RELABEL_WARPS>(RelabelDigit{deg}, RelabelPut{order, r.slot, r.pk, deg, init},
+                                                           n, nullptr, grid, order + order_words, s)));
     ctx->launches += 5;                  // count, three scan launches, scatter
     if (force) {
         BW_CUDA(cudaMemsetAsync(r.on, 1, sizeof(uint32_t), s));
     } else {
-        k_relabel_coverage<<<1, 1024, 0, s>>>(deg, order, std::min<uint64_t>(hubs, n), m, r.on);
-        ctx->launches++;
+        const uint64_t k = std::min<uint64_t>(hubs, n);
+        BW_CUDA(cudaMemsetAsync(cov, 0, 3 * sizeof(unsigned long long), s));
+        if (k) {
+            k_relabel_coverage<<<static_cast<unsigned>((k + 1023) / 1024), 1024, 0, s>>>(deg, order, k, m, cov, r.on);
+            ctx->launches++;
+        } else {
+            BW_CUDA(cudaMemsetAsync(r.on, 0, sizeof(uint32_t), s));
+        }
     }
-    if (first_translates) BW_CUDA(ctx_malloc_async(ctx, reinterpret_cast<void **>(&r.pk), n * sizeof(uint2), s));
-    k_relabel_slots<<<ctx->sm_count * 4, 256, 0, s>>>(order, n, r.on, r.slot, deg, r.pk);
-    ctx->launches++;
     if (m && !first_translates) {
         k_relabel_edges<<<ctx->sm_count * 8, 256, 0, s>>>(g->rev_edges, m, r.on, r.slot, r.gat_e);
         ctx->launches++;
