@@ -588,18 +588,24 @@ int bw_pagerank_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_sw
     cudaStream_t s = as_stream(stream);
     std::vector<float> hp(param_count(K));
     BW_CUDA(cudaMemcpyAsync(hp.data(), sw->params, hp.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
-    BW_CUDA(cudaStreamSynchronize(s));
     float ls = 0.f, lq = 0.f, lm = 0.f;
-    BW_TRY(pagerank_moments(ctx, g, &ls, &lq, &lm, s));
+    // also completes the parameter copy (it synchronises the stream)
+    if (const int rc = pagerank_moments(ctx, g, &ls, &lq, &lm, s); rc != BW_OK) {
+        cudaStreamSynchronize(s);        // hp must outlive the copy
+        return rc;
+    }
     // The features depend on the iteration index only, so the whole
-    // schedule is chosen before the run.
+    // schedule is chosen before the run; they take two values (the first
+    // iteration, every later one), so the network runs twice.
     std::vector<int32_t> sched(std::max<uint32_t>(iterations, 1u));
-    for (uint32_t it = 0; it < sched.size(); it++) {
+    int32_t choice[2];
+    for (uint32_t it = 0; it < 2; it++) {
         float x[F], probs[BW_MLP_MAX_CLASSES];
         pagerank_feature_vector(g, ls, lq, lm, it, x);
         mlp_forward_host(hp.data(), K, x, probs);
-        sched[it] = sw->candidates[pick(probs, K, sw->fallback, sw->threshold)];
+        choice[it] = sw->candidates[pick(probs, K, sw->fallback, sw->threshold)];
     }
+    for (uint32_t it = 0; it < sched.size(); it++) sched[it] = choice[it ? 1 : 0];
     if (schedule_out)
         for (uint32_t it = 0; it < iterations; it++) schedule_out[it] = sched[it];
     return pagerank_run_schedule_loop(ctx, g, sched.data(), static_cast<uint32_t>(sched.size()), iterations, ranks,
