@@ -1054,89 +1054,126 @@ __global__ void k_piece_emit(const uint32_t *__restrict__ off, const uint32_t *_
 
 // Short items are cut greedily over windows of 32 rows of rows[0, ne), in
 // order: an item ends before a long row (more than seg_long edges) and
-// before a row that would take it past SEG_EDGES edges.  One warp per
-// window: lane l loads row k0 + l (its length and first edge), then every
-// lane runs the same greedy walk over the shuffled lengths, so all lanes
-// hold the window's item starts and ends (bit l: an item starts at / ends
-// with row k0 + l).
-struct WindowRows {
-    uint32_t d, o;        // this lane's row: length, first edge
-    uint32_t starts, ends;
-};
-__device__ __forceinline__ WindowRows window_items(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                                                   uint64_t k0, uint64_t ne, uint32_t seg_long, unsigned lane)
+// before a row that would take it past SEG_EDGES edges.  A warp takes 32
+// consecutive windows: its lanes first load the 1024 rows' lengths and
+// first edges together into shared memory (row j of window i at i * 33 + j,
+// so that the lanes' walks below hit distinct banks), then lane l walks
+// window l from there.
+constexpr int SEG_WARPS = 4;
+constexpr uint32_t SEG_PAD = 33;
+constexpr uint32_t SEG_STAGE = 32 * SEG_PAD;                // words per warp and array
+
+__device__ __forceinline__ void stage_windows(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
+                                              uint64_t k0, uint64_t ne, uint32_t *s_d, uint32_t *s_o,
+                                              unsigned lane)
 {
-    WindowRows w{0u, 0u, 0u, 0u};
-    const uint32_t cnt = k0 < ne ? static_cast<uint32_t>(ne - k0 < 32 ? ne - k0 : 32) : 0u;
-    if (lane < cnt) {
-        const uint32_t r = rows[k0 + lane];
-        w.o = off[r];
-        w.d = off[r + 1] - w.o;
-    }
-    uint32_t acc_e = 0, acc_r = 0;
-    for (uint32_t l = 0; l < cnt; l++) {
-        const uint32_t dl = __shfl_sync(FULL_MASK, w.d, l);
-        if (dl > seg_long) {                         // long rows go to pieces
-            if (acc_r) { w.ends |= 1u << (l - 1); acc_r = 0; acc_e = 0; }
-            continue;
+#pragma unroll 4
+    for (uint32_t i = 0; i < 32; i++) {
+        const uint64_t k = k0 + i * 32 + lane;
+        uint32_t d = 0, o = 0;
+        if (k < ne) {
+            const uint32_t r = rows[k];
+            o = off[r];
+            d = off[r + 1] - o;
         }
-        if (acc_r && acc_e + dl > SEG_EDGES) { w.ends |= 1u << (l - 1); acc_r = 0; acc_e = 0; }
-        if (acc_r == 0) w.starts |= 1u << l;
-        acc_r++;
-        acc_e += dl;
+        s_d[i * SEG_PAD + lane] = d;
+        s_o[i * SEG_PAD + lane] = o;
     }
-    if (acc_r) w.ends |= 1u << (cnt - 1);
-    return w;
+    __syncwarp();
 }
 
 // counts[w]: the short items of window w; counts[W + w]: the CONST item of
 // window w of rows[ne, N).
-__global__ void k_seg_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                            const uint32_t *__restrict__ ne_dev, uint64_t n, uint32_t seg_long,
-                            uint32_t *__restrict__ counts)
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_count(const uint32_t *__restrict__ off,
+                                                              const uint32_t *__restrict__ rows,
+                                                              const uint32_t *__restrict__ ne_dev, uint64_t n,
+                                                              uint32_t seg_long, uint32_t *__restrict__ counts)
 {
+    __shared__ uint32_t s_d[SEG_WARPS * SEG_STAGE], s_o[SEG_WARPS * SEG_STAGE];
     const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
-    const unsigned lane = threadIdx.x & 31;
-    for (uint64_t w = gtid() >> 5; w < windows; w += gthreads() >> 5) {
-        const WindowRows wr = window_items(off, rows, w * 32, ne, seg_long, lane);
-        if (lane == 0) {
-            counts[w] = __popc(wr.starts);
-            counts[windows + w] = w * 32 < n - ne ? 1u : 0u;
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t *d_w = s_d + wib * SEG_STAGE, *o_w = s_o + wib * SEG_STAGE;
+    const uint64_t groups = (windows + 31) / 32, warps = gthreads() >> 5;
+    for (uint64_t gi = gtid() >> 5; gi < groups; gi += warps) {
+        stage_windows(off, rows, gi * 1024, ne, d_w, o_w, lane);
+        const uint64_t w = gi * 32 + lane;
+        if (w < windows) {
+            const uint64_t k0 = w * 32;
+            const uint32_t cnt = k0 < ne ? static_cast<uint32_t>(ne - k0 < 32 ? ne - k0 : 32) : 0u;
+            uint32_t items = 0, acc_e = 0, acc_r = 0;
+            for (uint32_t j = 0; j < cnt; j++) {
+                const uint32_t d = d_w[lane * SEG_PAD + j];
+                if (d > seg_long) {                     // long rows go to pieces
+                    if (acc_r) { items++; acc_r = 0; acc_e = 0; }
+                    continue;
+                }
+                if (acc_r && acc_e + d > SEG_EDGES) { items++; acc_r = 0; acc_e = 0; }
+                acc_r++;
+                acc_e += d;
+            }
+            if (acc_r) items++;
+            counts[w] = items;
+            counts[windows + w] = k0 < n - ne ? 1u : 0u;
         }
+        __syncwarp();
     }
 }
 
 // Short items {k0, k1, e0, e1} over rows[k0, k1) (their edges are
 // contiguous: rows in between have none); CONST items
 // {ne + k0, ne + k1 | CONST, 0, 0}; both after the P pieces.
-__global__ void k_seg_emit(const uint32_t *__restrict__ off, const uint32_t *__restrict__ rows,
-                           const uint32_t *__restrict__ ne_dev, uint64_t n, uint32_t seg_long,
-                           const uint32_t *__restrict__ first,
-                           const uint32_t *__restrict__ piece_total, uint4 *__restrict__ work,
-                           uint32_t *__restrict__ tot)
+__global__ void __launch_bounds__(SEG_WARPS * 32) k_seg_emit(const uint32_t *__restrict__ off,
+                                                             const uint32_t *__restrict__ rows,
+                                                             const uint32_t *__restrict__ ne_dev, uint64_t n,
+                                                             uint32_t seg_long, const uint32_t *__restrict__ first,
+                                                             const uint32_t *__restrict__ piece_total,
+                                                             uint4 *__restrict__ work, uint32_t *__restrict__ tot)
 {
+    __shared__ uint32_t s_d[SEG_WARPS * SEG_STAGE], s_o[SEG_WARPS * SEG_STAGE];
     const uint64_t windows = (n + 31) / 32, ne = *ne_dev;
     const uint32_t P = *piece_total;
-    const unsigned lane = threadIdx.x & 31;
+    const unsigned lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (gtid() == 0) {
         tot[0] = P + first[windows];
         tot[1] = P + first[2 * windows];
     }
-    for (uint64_t w = gtid() >> 5; w < windows; w += gthreads() >> 5) {
-        const uint64_t k0 = w * 32;
-        const WindowRows wr = window_items(off, rows, k0, ne, seg_long, lane);
-        // an item starting at this lane ends with the first end at or after it
-        const bool start = (wr.starts >> lane) & 1u;
-        const uint32_t below = (1u << lane) - 1u;
-        const uint32_t e = start ? static_cast<uint32_t>(__ffs(wr.ends & ~below) - 1) : lane;
-        const uint32_t oe = __shfl_sync(FULL_MASK, wr.o, e), de = __shfl_sync(FULL_MASK, wr.d, e);
-        if (start)
-            work[P + first[w] + __popc(wr.starts & below)] =
-                make_uint4(static_cast<uint32_t>(k0 + lane), static_cast<uint32_t>(k0 + e + 1), wr.o, oe + de);
-        if (lane == 0 && k0 < n - ne) {
-            const uint64_t c0 = ne + k0, c1 = min(n, c0 + 32);
-            work[P + first[windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
+    uint32_t *d_w = s_d + wib * SEG_STAGE, *o_w = s_o + wib * SEG_STAGE;
+    const uint64_t groups = (windows + 31) / 32, warps = gthreads() >> 5;
+    for (uint64_t gi = gtid() >> 5; gi < groups; gi += warps) {
+        stage_windows(off, rows, gi * 1024, ne, d_w, o_w, lane);
+        const uint64_t w = gi * 32 + lane;
+        if (w < windows) {
+            const uint64_t k0 = w * 32;
+            const uint32_t cnt = k0 < ne ? static_cast<uint32_t>(ne - k0 < 32 ? ne - k0 : 32) : 0u;
+            const uint32_t *dr = d_w + lane * SEG_PAD, *orow = o_w + lane * SEG_PAD;
+            uint32_t out = P + first[w];
+            uint32_t start = 0, acc_e = 0, acc_r = 0;
+            for (uint32_t j = 0; j < cnt; j++) {
+                const uint32_t d = dr[j];
+                if (d > seg_long) {
+                    if (acc_r) {
+                        work[out++] = make_uint4(uint32_t(k0 + start), uint32_t(k0 + j), orow[start], orow[j]);
+                        acc_r = 0; acc_e = 0;
+                    }
+                    continue;
+                }
+                if (acc_r && acc_e + d > SEG_EDGES) {
+                    work[out++] = make_uint4(uint32_t(k0 + start), uint32_t(k0 + j), orow[start], orow[j]);
+                    acc_r = 0; acc_e = 0;
+                }
+                if (acc_r == 0) start = j;
+                acc_r++;
+                acc_e += d;
+            }
+            if (acc_r)
+                work[out++] = make_uint4(uint32_t(k0 + start), uint32_t(k0 + cnt), orow[start],
+                                         orow[cnt - 1] + dr[cnt - 1]);
+            if (k0 < n - ne) {
+                const uint64_t c0 = ne + k0, c1 = min(n, c0 + 32);
+                work[P + first[windows + w]] = make_uint4(uint32_t(c0), uint32_t(c1) | CONST_FLAG, 0u, 0u);
+            }
         }
+        __syncwarp();
     }
 }
 
@@ -1971,11 +2008,16 @@ int build_segments(bw_context *ctx, const bw_graph_view *g, uint32_t seg_long, P
     k_piece_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.long_rows, long_len, run.long_total, ppos,
                                       run.work, run.long_count, run.giant_total, run.giant_pieces);
     BW_CUDA(cudaMemsetAsync(run.sum_ctr, 0, 2 * sizeof(uint32_t), s));
-    // 3. short and CONST items after the pieces
-    k_seg_count<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, wcnt);
+    // 3. short and CONST items after the pieces: a warp per 32 windows of
+    //    32 rows
+    const uint64_t seg_warps = (windows + 31) / 32;
+    const unsigned seg_grid = static_cast<unsigned>(
+        std::min<uint64_t>((seg_warps + SEG_WARPS - 1) / SEG_WARPS, uint64_t(ctx->sm_count) * 32));
+    k_seg_count<<<seg_grid, SEG_WARPS * 32, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, wcnt);
     BW_CUDA(cudaMemsetAsync(wcnt + 2 * windows, 0, sizeof(uint32_t), s));
     BW_CUDA(sortk::scan_exclusive(wcnt, first, 2 * windows + 1, part, s));
-    k_seg_emit<<<grid, 256, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, first, ppos + lcap, run.work, tot);
+    k_seg_emit<<<seg_grid, SEG_WARPS * 32, 0, s>>>(g->rev_vertices, run.rows, ne, n, seg_long, first, ppos + lcap,
+                                                  run.work, tot);
     // rows count/partition, two tile scans, sort 4, piece count/scan 3/emit, seg count/scan 3/emit
     ctx->launches += 20;
     BW_CUDA(cudaGetLastError());
