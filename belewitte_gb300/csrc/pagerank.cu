@@ -886,9 +886,14 @@ constexpr int PULL_WIDE = 1024, PULL_NARROW = 256;
 constexpr uint32_t PULL_BUF = SEG_EDGES;
 constexpr size_t pull_fixed_smem(int block) { return (block / 32) * (PULL_BUF + 33) * sizeof(float); }
 constexpr int pull_min_blocks(int block) { return block == PULL_WIDE ? 1 : 4; }
-// default hub-cache entries per block (measured on GB300: WIDE with 16K
-// entries is within 3% of the best shape on both R-MAT-22 and ER(4M, 67M))
-constexpr uint32_t PULL_WIDE_HUBS = 16384, PULL_NARROW_HUBS = 0;
+// Default hub-cache entries per block.  WIDE's fixed buffers (69,760 bytes)
+// with 16K entries already take the 164 KB shared-memory carveout; 24,288
+// entries fill it (with the 1 KB the system reserves per block), so L1
+// keeps the same 92 KB.  Measured on GB300 (vertex-pull, us per iteration):
+// R-MAT-22 16K 323.0, 20K 320.0, 24,288 317.9, 28K 315.9, 32K 381.4;
+// ER(4M, 67M) 276.9, 277.0, 277.0, 281.2, 505.3 -- from 32K the carveout
+// grows to 228 KB and the 28 KB left to L1 cannot hold the gathers in flight.
+constexpr uint32_t PULL_WIDE_HUBS = 24288, PULL_NARROW_HUBS = 0;
 constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 
 // Work-list construction.
