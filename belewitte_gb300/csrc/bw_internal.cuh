@@ -79,6 +79,14 @@ __host__ __device__ __forceinline__ unsigned long long lsq_fx(float l)
 }
 __host__ __device__ __forceinline__ double lsum_value(unsigned long long v) { return static_cast<double>(v) / LSUM_UNIT; }
 __host__ __device__ __forceinline__ double lsq_value(unsigned long long v) { return static_cast<double>(v) / LSQ_UNIT; }
+// The moments as the features read them: rounded to IEEE single, the
+// precision the level statistics report them in (bw_bfs_level_stats), so
+// the device switch, the host loop, the training samples and a predictor
+// library fed the reported statistics all form identical features.
+__host__ __device__ __forceinline__ double lsum_feature(unsigned long long v)
+{ return static_cast<double>(static_cast<float>(lsum_value(v))); }
+__host__ __device__ __forceinline__ double lsq_feature(unsigned long long v)
+{ return static_cast<double>(static_cast<float>(lsq_value(v))); }
 
 struct BfsCtl {
     LevelSlot slot[3];

@@ -376,8 +376,8 @@ __global__ void __launch_bounds__(PREDICT_THREADS) k_bfs_predict(PredictArgs a)
         const LevelSlot s = c->slot[(L + 2) % 3];
         float lmax;
         memcpy(&lmax, &s.lmax_bits, 4);
-        bwfeat::compute(static_cast<double>(s.frontier), static_cast<double>(s.fedges), lsum_value(s.lsum),
-                        lsq_value(s.lsq), lmax,
+        bwfeat::compute(static_cast<double>(s.frontier), static_cast<double>(s.fedges), lsum_feature(s.lsum),
+                        lsq_feature(s.lsq), lmax,
                         static_cast<double>(a.n), static_cast<double>(a.m), static_cast<double>(c->visited),
                         static_cast<double>(c->traversed), static_cast<double>(L), x);
     }
@@ -749,7 +749,7 @@ int bw_bfs_profile(bw_context *ctx, const bw_graph_view *g, uint32_t root, int32
     for (; L < max_levels; L++) {
         float lmax;
         std::memcpy(&lmax, &cur.lmax_bits, 4);
-        bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_value(cur.lsum), lsq_value(cur.lsq), lmax,
+        bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_feature(cur.lsum), lsq_feature(cur.lsq), lmax,
                         static_cast<double>(n),
                         static_cast<double>(m), static_cast<double>(visited), static_cast<double>(edges_visited), L,
                         features + static_cast<size_t>(L) * F);
@@ -836,7 +836,7 @@ int bw_bfs_run_learned(bw_context *ctx, const bw_graph_view *g, const bw_switch_
             if (L >= max_levels) { rc = BW_ERR_LEVEL_LIMIT; break; }
             float x[F], probs[BW_MLP_MAX_CLASSES], lmax;
             std::memcpy(&lmax, &cur.lmax_bits, 4);
-            bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_value(cur.lsum), lsq_value(cur.lsq), lmax,
+            bwfeat::compute(cur.frontier, static_cast<double>(cur.fedges), lsum_feature(cur.lsum), lsq_feature(cur.lsq), lmax,
                             static_cast<double>(n), static_cast<double>(m), static_cast<double>(visited),
                             static_cast<double>(edges_visited), L, x);
             mlp_forward_host(hp.data(), K, x, probs);

@@ -233,8 +233,9 @@ def test_kernel_runner_switch_with_exported_predictor(predictor_so, tmp_path):
     ids = [bw.bfs_variant_id(c) for c in pred.candidates]
     chosen = [ids.index(s["variant"]) for s in run.level_stats]
     got = [preds[L] for L in range(len(chosen))]
-    # Level statistics are float sums accumulated in any order, so a
-    # near-tie can fall either way; all but one level must agree.
-    agree = sum(a == b for a, b in zip(got, chosen))
-    assert agree >= len(chosen) - 1, (got, chosen)
+    # The level statistics are fixed-point sums (the same whatever order the
+    # threads added in), the switch and the exported library both form the
+    # features from them rounded to single precision, and both run the same
+    # host network: every level's choice agrees.
+    assert got == chosen, (got, chosen)
     torch.cuda.synchronize()
