@@ -233,13 +233,14 @@ typedef struct bw_launch_config {
  * Work-list PageRank variants (vertex-pull, vertex-pull-nodiv,
  * pull-segmented): block_size 1024 (default) or 256 picks the block shape,
  * chunk_size the number of gathered-array entries each block caches in
- * shared memory (0 = default, multiple of 4), warp_size the long-row
+ * shared memory (0 = default: 24,288 for block_size 1024, none for 256;
+ * a multiple of 4), warp_size the long-row
  * threshold (0 = 256, at most 512): rows with more in-edges are cut into
  * pieces whose sequential sums a second kernel evaluates, shorter ones are
  * summed where they are gathered.  Relabelling stores the
  * gathered array in decreasing out-degree order so that the cached entries
- * are the hubs; it costs one pass over the edges per run and leaves every
- * result unchanged.  By default it runs when the cached entries would cover
+ * are the hubs; it costs one gather per edge per run (for the div variants
+ * inside their first iteration) and leaves every result unchanged.  By default it runs when the cached entries would cover
  * at least 5% more of the edges than in vertex order (and the run has at
  * least 4 iterations); BW_LAUNCH_RELABEL forces it, BW_LAUNCH_NO_RELABEL
  * turns it off.
@@ -409,7 +410,7 @@ typedef struct bw_pagerank_result {
     uint32_t kernel_launches; /* this library's kernels launched by the run */
     float last_diff;        /* sum |pr_new - pr_old| of the last iteration */
     float reserved_f;
-    double device_ms;       /* degrees + all iterations on the device */
+    double device_ms;       /* the whole run on the device: degrees, set-up, iterations */
 } bw_pagerank_result;
 
 /*
