@@ -903,8 +903,9 @@ constexpr int GATHER_UNROLL = 16;   // 512 edges = one unrolled round
 //    in-edges become CONST items at the end of the list (for the div
 //    variants their rank and contribution are the same from the second
 //    iteration on, so later iterations leave them out).
-//  * Long rows (more edges than the threshold) are sorted by decreasing length
-//    and cut into SEG_EDGES pieces in that order, at the front of the list.
+//  * Long rows (more edges than the threshold) are put in decreasing length
+//    order (long_row_key) and cut into SEG_EDGES pieces in that order, at
+//    the front of the list.
 // Layout: [pieces | short items | CONST items]; the lengths stay on the
 // device (tot[0] = items before the CONST ones, tot[1] = all items).
 // Tile b of SCAN_TILE rows: part_e[b] rows with in-edges, part_l[b] long rows.
